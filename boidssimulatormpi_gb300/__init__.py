@@ -1,0 +1,264 @@
+"""GB300-native per-timestep boid update (drop-in for maru-n/BoidsSimulatorMPI).
+
+The compute lives in ``libboids_gb300.so`` (hand-written sm_103a kernels
+behind the C ABI of ``include/boids.h``).  This module binds that ABI with
+ctypes and mirrors the reference's ``BoidSimulation`` interface
+(src/boid_simulation.h:15-71): ``setup`` / ``init`` / ``update`` / ``get`` /
+``get_v`` / ``get_force``, plus bulk accessors.  There is no CPU fallback:
+importing the bindings fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "libboids_gb300.so")
+
+ENGINE_ALLPAIRS = 0
+ENGINE_GRID = 1
+FLAG_RECORD_FORCES = 1
+
+ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "EIO", -5: "ESTATE", -6: "ENOTSUP"}
+
+
+class BoidsError(RuntimeError):
+    """A negative status from the C ABI; ``code`` is the status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [("number_of_agents", C.c_uint32), ("field_size", C.c_double),
+                ("separation_sight_distance", C.c_double), ("separation_sight_angle", C.c_double),
+                ("separation_force_coefficient", C.c_double),
+                ("alignment_sight_distance", C.c_double), ("alignment_sight_angle", C.c_double),
+                ("alignment_force_coefficient", C.c_double),
+                ("cohesion_sight_distance", C.c_double), ("cohesion_sight_angle", C.c_double),
+                ("cohesion_force_coefficient", C.c_double),
+                ("velocity_max", C.c_double), ("velocity_min", C.c_double),
+                ("engine", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class GridInfo(C.Structure):
+    _fields_ = [("ref_interaction_range", C.c_float), ("ref_grid_num", C.c_int32),
+                ("ref_grid_size", C.c_float), ("dev_cells_per_axis", C.c_int32),
+                ("dev_cell_size", C.c_float), ("list_capacity", C.c_int32)]
+
+
+class Profile(C.Structure):
+    _fields_ = [("bin_ms", C.c_double), ("force_ms", C.c_double), ("other_ms", C.c_double),
+                ("steps", C.c_uint64), ("force_launches", C.c_uint64), ("bin_launches", C.c_uint64)]
+
+
+# Every symbol include/boids.h declares, with its ctypes signature.
+_vp = C.c_void_p
+SIGNATURES = {
+    "boids_create": (C.c_int, [C.POINTER(Params), C.POINTER(_vp)]),
+    "boids_destroy": (None, [_vp]),
+    "boids_init": (C.c_int, [_vp, C.c_char_p, C.c_int32]),
+    "boids_init_ex": (C.c_int, [_vp, C.c_char_p, C.c_int32, C.c_int32]),
+    "boids_set_state": (C.c_int, [_vp, _vp, _vp]),
+    "boids_step": (C.c_int, [_vp, C.c_int32]),
+    "boids_get_state": (C.c_int, [_vp, _vp, _vp]),
+    "boids_get_forces": (C.c_int, [_vp, _vp]),
+    "boids_get_cells": (C.c_int, [_vp, _vp]),
+    "boids_get_neighbor_sets": (C.c_int, [_vp, _vp, _vp]),
+    "boids_get_grid_info": (C.c_int, [_vp, C.POINTER(GridInfo)]),
+    "boids_set_stream": (C.c_int, [_vp, _vp]),
+    "boids_synchronize": (C.c_int, [_vp]),
+    "boids_profile_enable": (C.c_int, [_vp, C.c_int32]),
+    "boids_profile_read": (C.c_int, [_vp, C.POINTER(Profile), C.c_int32]),
+    "boids_kernel_launches": (C.c_uint64, [_vp]),
+    "boids_last_error": (C.c_char_p, []),
+    "boids_version": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+def lib():
+    """Loads libboids_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libboids_gb300.so is not built: run "
+                               "`python -c 'import __graft_entry__ as g; g.build()'` or "
+                               "`python boidssimulatormpi_gb300/build.py`")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise BoidsError(rc, lib().boids_last_error().decode())
+
+
+def _f32(a, n):
+    a = np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+    if a.size != n:
+        raise ValueError("expected %d floats, got %d" % (n, a.size))
+    return a
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class BoidSimulation:
+    """Mirror of the reference's BoidSimulation over the C ABI.
+
+    ``engine`` picks the link-time variant the reference has: "grid"
+    (boidsim_grid, src/boid_simulation_grid.cpp) or "allpairs" (boidsim,
+    src/boid_simulation.cpp).
+    """
+
+    def __init__(self, engine: str = "grid", device: int = 0, record_forces: bool = False):
+        self.engine = {"grid": ENGINE_GRID, "allpairs": ENGINE_ALLPAIRS}[engine]
+        self.device = device
+        self.record_forces = record_forces
+        self.h = None
+        self.N = 0
+        self._cache = None
+
+    # -- BoidSimulation::setup (src/boid_simulation.h:19-33)
+    def setup(self, number_of_agents, field_size,
+              separation_sight_distance, separation_sight_angle, separation_force_coefficient,
+              alignment_sight_distance, alignment_sight_angle, alignment_force_coefficient,
+              cohesion_sight_distance, cohesion_sight_angle, cohesion_force_coefficient,
+              velocity_max, velocity_min, initialization="random_uniform", rand_seed=12345):
+        self.close()
+        p = Params(number_of_agents, field_size,
+                   separation_sight_distance, separation_sight_angle, separation_force_coefficient,
+                   alignment_sight_distance, alignment_sight_angle, alignment_force_coefficient,
+                   cohesion_sight_distance, cohesion_sight_angle, cohesion_force_coefficient,
+                   velocity_max, velocity_min, self.engine, self.device,
+                   FLAG_RECORD_FORCES if self.record_forces else 0, 0)
+        h = C.c_void_p()
+        _check(lib().boids_create(C.byref(p), C.byref(h)))
+        self.h = h
+        self.params = p
+        self.N = number_of_agents
+        self.field_size_X = self.field_size_Y = self.field_size_Z = float(field_size)
+        self.initialization_type = initialization
+        self.rand_seed = rand_seed
+        self.time_step = 0
+        return self
+
+    # -- BoidSimulation::init
+    def init(self, seed_mode: int = -1):
+        _check(lib().boids_init_ex(self.h, self.initialization_type.encode(), self.rand_seed, seed_mode))
+        self._cache = None
+
+    # -- BoidSimulation::update
+    def update(self, steps: int = 1):
+        _check(lib().boids_step(self.h, steps))
+        self._cache = None
+
+    step = update
+
+    def set_state(self, pos, vel):
+        pos, vel = _f32(pos, 3 * self.N), _f32(vel, 3 * self.N)
+        _check(lib().boids_set_state(self.h, _ptr(pos), _ptr(vel)))
+        self._cache = None
+
+    def state(self, pos_out=None, vel_out=None):
+        """(pos, vel) as float32 arrays of shape (N, 3), id order."""
+        pos = np.empty(3 * self.N, np.float32) if pos_out is None else pos_out
+        vel = np.empty(3 * self.N, np.float32) if vel_out is None else vel_out
+        _check(lib().boids_get_state(self.h, _ptr(pos), _ptr(vel)))
+        return pos.reshape(self.N, 3), vel.reshape(self.N, 3)
+
+    def positions(self, out=None):
+        pos = np.empty(3 * self.N, np.float32) if out is None else out
+        _check(lib().boids_get_state(self.h, _ptr(pos), None))
+        return pos.reshape(self.N, 3)
+
+    def forces(self):
+        """get_force for all ids: (N, 9) = cohesion xyz, separation xyz, alignment xyz."""
+        f = np.empty(9 * self.N, np.float32)
+        _check(lib().boids_get_forces(self.h, _ptr(f)))
+        return f.reshape(self.N, 9)
+
+    def cells(self):
+        """Boid::grid_index[8] of every boid, (N, 8) int32."""
+        g = np.empty(8 * self.N, np.int32)
+        _check(lib().boids_get_cells(self.h, _ptr(g)))
+        return g.reshape(self.N, 8)
+
+    def neighbor_sets(self):
+        """(count, hash), each (N, 3): per rule (cohesion, separation, alignment)."""
+        c = np.empty(3 * self.N, np.int32)
+        h = np.empty(3 * self.N, np.uint64)
+        _check(lib().boids_get_neighbor_sets(self.h, _ptr(c), _ptr(h)))
+        return c.reshape(self.N, 3), h.reshape(self.N, 3)
+
+    def grid_info(self) -> dict:
+        gi = GridInfo()
+        _check(lib().boids_get_grid_info(self.h, C.byref(gi)))
+        return {f: getattr(gi, f) for f, _ in GridInfo._fields_}
+
+    def set_stream(self, stream_handle: int | None):
+        _check(lib().boids_set_stream(self.h, C.c_void_p(stream_handle) if stream_handle else None))
+
+    def synchronize(self):
+        _check(lib().boids_synchronize(self.h))
+
+    def profile_enable(self, on=True):
+        _check(lib().boids_profile_enable(self.h, int(on)))
+
+    def profile_read(self, reset=True) -> dict:
+        pr = Profile()
+        _check(lib().boids_profile_read(self.h, C.byref(pr), int(reset)))
+        return {f: getattr(pr, f) for f, _ in Profile._fields_}
+
+    def kernel_launches(self) -> int:
+        return int(lib().boids_kernel_launches(self.h))
+
+    # -- per-id getters of the reference (src/boid_simulation.h:37-43)
+    def _state_cached(self):
+        if self._cache is None:
+            self._cache = self.state()
+        return self._cache
+
+    def get(self, i):
+        p, _ = self._state_cached()
+        return tuple(float(x) for x in p[i])
+
+    def get_v(self, i):
+        _, v = self._state_cached()
+        return tuple(float(x) for x in v[i])
+
+    def get_force(self, i):
+        return tuple(float(x) for x in self.forces()[i])
+
+    def close(self):
+        if self.h is not None and _lib is not None:
+            _lib.boids_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def version() -> str:
+    return lib().boids_version().decode()

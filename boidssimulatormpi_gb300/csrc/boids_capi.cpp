@@ -1,0 +1,655 @@
+// boids_capi.cpp -- the C ABI of include/boids.h: engine set-up, state
+// transfer, stepping and diagnostics.  The compute is in boids_kernels.cu;
+// this file owns the handle, its device memory and its stream.
+//
+// Built with -ffp-contract=off: the host-side initial-state draws must round
+// like the reference's x86 build on any host (aarch64 contracts to FMA by
+// default).
+#include "boids.h"
+#include "boids_engine.h"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <algorithm>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+
+using boidsgpu::DevBuffers;
+using boidsgpu::RuleConst;
+using boidsgpu::StepConst;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *where)
+{
+    return fail(BOIDS_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                              \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+    } while (0)
+
+// ------------------------------------------------------------------ exact float thresholds
+
+float f_dn(double d)  // largest float <= d
+{
+    float f = (float)d;
+    if ((double)f > d) f = std::nextafter(f, -INFINITY);
+    return f;
+}
+
+float f_up(double d)  // smallest float >= d
+{
+    float f = (float)d;
+    if ((double)f < d) f = std::nextafter(f, INFINITY);
+    return f;
+}
+
+int64_t ordinal(float x)
+{
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    return (u & 0x80000000u) ? -(int64_t)(u & 0x7fffffffu) : (int64_t)u;
+}
+
+float from_ordinal(int64_t o)
+{
+    uint32_t u = o < 0 ? (uint32_t)(-o) | 0x80000000u : (uint32_t)o;
+    float x;
+    std::memcpy(&x, &u, 4);
+    return x;
+}
+
+// Boid::isInsideArea's cone test is (double)acosf(c) <= M_PI*a with c a
+// float (src/boid.cpp:34-35).  With acosf non-increasing on [-1, 1] the set
+// of passing c is [cstar, 1]; cstar is found by bisection over the floats
+// with the host's own acosf -- the function the reference calls -- and the
+// monotonicity is re-checked in a window around it.
+int cone_threshold(double a, float *cstar)
+{
+    const double T = M_PI * a;
+    auto ok = [T](float c) { return (double)std::acos(c) <= T; };  // float overload: acosf
+    if (!ok(1.0f)) { *cstar = INFINITY; return 0; }
+    if (ok(-1.0f)) { *cstar = -1.0f; return 0; }
+    int64_t lo = ordinal(-1.0f), hi = ordinal(1.0f);  // ok(lo) false, ok(hi) true
+    while (hi - lo > 1) {
+        const int64_t mid = lo + (hi - lo) / 2;
+        if (ok(from_ordinal(mid))) hi = mid; else lo = mid;
+    }
+    for (int64_t o = hi - 4096; o < hi + 4096; ++o) {
+        if (o < ordinal(-1.0f) || o > ordinal(1.0f)) continue;
+        if (ok(from_ordinal(o)) != (o >= hi))
+            return fail(BOIDS_ENOTSUP, "host acosf is not monotone near the view-cone threshold");
+    }
+    *cstar = from_ordinal(hi);
+    return 0;
+}
+
+// The radius test (double)sqrtf(d2) < r (src/boid.cpp:28, with
+// Vector3D::norm at src/vector3D.cpp:64-67).  sqrtf is correctly rounded,
+// hence monotone, so the passing d2 are [0, lim) for the float lim returned.
+float radius_d2_limit(double r)
+{
+    auto inside = [r](float d2) { return (double)std::sqrt(d2) < r; };  // float overload: sqrtf
+    if (!inside(0.0f)) return 0.0f;
+    if (inside(INFINITY)) return INFINITY;
+    int64_t lo = 0, hi = ordinal(INFINITY);  // inside(lo), !inside(hi)
+    while (hi - lo > 1) {
+        const int64_t mid = lo + (hi - lo) / 2;
+        if (inside(from_ordinal(mid))) lo = mid; else hi = mid;
+    }
+    return from_ordinal(hi);
+}
+
+// ------------------------------------------------------------------ drand48
+
+struct Drand48 {
+    uint64_t x = 0;  // glibc's state before any srand48 call
+    void seed(long s) { x = (((uint64_t)s & 0xffffffffULL) << 16) | 0x330eULL; }
+    double next()
+    {
+        x = (0x5deece66dULL * x + 0xbULL) & 0xffffffffffffULL;
+        return (double)x * (1.0 / 281474976710656.0);
+    }
+};
+
+}  // namespace
+
+// ------------------------------------------------------------------ handle
+
+struct boids_sim {
+    boids_params p{};
+    StepConst k{};
+    DevBuffers b{};
+    int engine = 0;        // effective kernels: 0 all-pairs, 1 device grid
+    bool ref_geometry_ok = false;
+    int cur = 0;           // buffer holding the state
+    bool has_state = false;
+    bool forces_valid = false;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    uint64_t launches = 0;
+    uint64_t steps_done = 0;
+    // profiling: event pairs recorded around each phase, resolved on read
+    struct Pending {
+        cudaEvent_t a, b;
+        int slot;  // 0 bin, 1 force, 2 other
+    };
+    bool prof = false;
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> pool;
+    boids_profile_t acc{};
+};
+
+namespace {
+
+void free_buffers(DevBuffers &b)
+{
+    void *ptrs[] = {b.pos[0], b.pos[1], b.vel[0], b.vel[1], b.key, b.rank, b.count, b.lstart,
+                    b.bsum, b.ticket, b.ap_cnt, b.ap_list, b.forces, b.stage, b.cells8, b.dcnt, b.dhash,
+                    b.dense_list, b.dense_n};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    b = DevBuffers{};
+}
+
+template <class T>
+int dalloc(T **p, size_t count, bool zero = false)
+{
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, sizeof(T) * count);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(BOIDS_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    if (zero) {
+        e = cudaMemset(*p, 0, sizeof(T) * count);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
+    }
+    return 0;
+}
+
+int use_device(boids_sim *s)
+{
+    cudaError_t e = cudaSetDevice(s->p.device);
+    return e == cudaSuccess ? 0 : cuda_fail(e, "cudaSetDevice");
+}
+
+// Reference grid sizing, src/boid_simulation_grid.cpp:80-89.
+bool ref_geometry(const boids_params &p, float *R, int *G, float *GS)
+{
+    double m = (p.cohesion_sight_distance < p.alignment_sight_distance) ? p.alignment_sight_distance
+                                                                         : p.cohesion_sight_distance;
+    m = (m < p.separation_sight_distance) ? p.separation_sight_distance : m;
+    const float r = (float)m;
+    const int gn = (int)(p.field_size / (double)(r * 2));
+    if (gn <= 0) return false;
+    const unsigned g = (unsigned)gn;
+    const float gs = (float)(p.field_size / (double)g);
+    if (r * 2 >= gs) return false;
+    *R = r;
+    *G = gn;
+    *GS = gs;
+    return true;
+}
+
+cudaEvent_t take_event(boids_sim *s)
+{
+    if (!s->pool.empty()) {
+        cudaEvent_t e = s->pool.back();
+        s->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Adds the elapsed time of every recorded phase to the totals.
+void resolve_events(boids_sim *s)
+{
+    for (auto &q : s->pending) {
+        float ms = 0.f;
+        cudaEventSynchronize(q.b);
+        if (cudaEventElapsedTime(&ms, q.a, q.b) == cudaSuccess) {
+            double *slot = q.slot == 0 ? &s->acc.bin_ms : q.slot == 1 ? &s->acc.force_ms : &s->acc.other_ms;
+            *slot += ms;
+        }
+        s->pool.push_back(q.a);
+        s->pool.push_back(q.b);
+    }
+    s->pending.clear();
+}
+
+// Brackets the launches of one phase with events on the handle's stream.
+struct PhaseTimer {
+    boids_sim *s;
+    int slot;
+    cudaEvent_t a = nullptr;
+    PhaseTimer(boids_sim *s_, int slot_) : s(s_), slot(slot_)
+    {
+        if (!s->prof) return;
+        if (s->pending.size() > 8192) resolve_events(s);
+        a = take_event(s);
+        cudaEventRecord(a, s->stream);
+    }
+    ~PhaseTimer()
+    {
+        if (!a) return;
+        cudaEvent_t b = take_event(s);
+        cudaEventRecord(b, s->stream);
+        s->pending.push_back({a, b, slot});
+    }
+};
+
+int grid_bin_fresh(boids_sim *s)
+{
+    CK(cudaMemsetAsync(s->b.count, 0, sizeof(uint32_t) * s->b.ncell_pad, s->stream));
+    CK(boidsgpu::launch_grid_keys(s->k, s->b.pos[s->cur], s->b.key, s->b.rank, s->b.count, s->stream,
+                                  &s->launches));
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *boids_last_error(void) { return g_err.c_str(); }
+
+const char *boids_version(void) { return "boids_gb300 0.1 (sm_103a)"; }
+
+int boids_create(const boids_params *params, boids_sim **out)
+{
+    if (!params || !out) return fail(BOIDS_EINVAL, "boids_create: null argument");
+    *out = nullptr;
+    const boids_params &p = *params;
+    if (p.number_of_agents > boidsgpu::kMaxBoids)
+        return fail(BOIDS_EINVAL, "number_of_agents exceeds 2^29");
+    if (!(p.field_size > 0.0) || !std::isfinite(p.field_size))
+        return fail(BOIDS_EINVAL, "field_size must be positive and finite");
+    if (p.engine != BOIDS_ENGINE_ALLPAIRS && p.engine != BOIDS_ENGINE_GRID)
+        return fail(BOIDS_EINVAL, "unknown engine");
+    const double radii[3] = {p.cohesion_sight_distance, p.separation_sight_distance, p.alignment_sight_distance};
+    for (double r : radii)
+        if (std::isnan(r)) return fail(BOIDS_EINVAL, "sight distance is NaN");
+
+    boids_sim *s = new boids_sim();
+    s->p = p;
+    StepConst &k = s->k;
+    k.n = p.number_of_agents;
+    k.F = p.field_size;
+    k.Ff = (float)p.field_size;
+    k.F_dn = f_dn(p.field_size);
+    k.halfF_dn = f_dn(p.field_size / 2);
+    k.halfFf = (float)(p.field_size / 2);
+    k.cc = (float)p.cohesion_force_coefficient;
+    k.cs = (float)p.separation_force_coefficient;
+    k.ca = (float)p.alignment_force_coefficient;
+    k.vmax_dn = f_dn(p.velocity_max);
+    k.vmin_up = f_up(p.velocity_min);
+    k.vmax_f = (float)p.velocity_max;
+    k.vmin_f = (float)p.velocity_min;
+    k.Fsd = boidsgpu::soft_double(p.field_size);
+    k.cone_band = 4e-6f;
+    {
+        int bits = 0;
+        while (bits < 32 && (1ull << bits) < (uint64_t)(k.n ? k.n : 1)) ++bits;
+        k.id_bits = std::max(4, (bits + 3) / 4 * 4);
+    }
+    const double ang[3] = {p.cohesion_sight_angle, p.separation_sight_angle, p.alignment_sight_angle};
+    float rmax = 0.f;
+    k.d2_any = 0.f;
+    for (int r = 0; r < 3; ++r) {
+        RuleConst &q = k.rule[r];
+        q.d2_lim = radius_d2_limit(radii[r]);
+        q.all_round = ang[r] >= 1.0;
+        q.cstar = INFINITY;
+        if (!q.all_round) {
+            int rc = cone_threshold(ang[r], &q.cstar);
+            if (rc) { delete s; return rc; }
+        }
+        k.d2_any = std::fmax(k.d2_any, q.d2_lim);
+        const float rup = f_up(radii[r]);
+        if (rup > rmax) rmax = rup;
+    }
+    // Conservative filter radius: the exact distance test can only accept a
+    // pair whose approximate distance is below this (rounding of the image
+    // shift and of the filter's own arithmetic is far below the margin).
+    const double ulpF = std::nextafter(std::fmax(k.Ff, 1.0f), INFINITY) - std::fmax(k.Ff, 1.0f);
+    const double rf = (double)rmax * (1.0 + 1e-4) + 8.0 * ulpF;
+    k.filt_r2 = (float)(rf * rf);
+    k.box_lim = (float)(p.field_size / 2 - rf * (1.0 + 1e-4) - 8.0 * ulpF);
+
+    // reference overlapping-grid geometry
+    float refR = 0.f, refGS = 0.f;
+    int refG = 0;
+    s->ref_geometry_ok = ref_geometry(p, &refR, &refG, &refGS);
+    if (p.engine == BOIDS_ENGINE_GRID) {
+        if (!s->ref_geometry_ok) {
+            delete s;
+            return fail(BOIDS_EINVAL, "Invalid GRID_NUM: the reference grid engine needs "
+                                      "field_size > 2 * max sight distance (src/boid_simulation_grid.cpp:86-89)");
+        }
+        if (refG == 1) {
+            delete s;
+            return fail(BOIDS_EINVAL, "GRID_NUM == 1: the reference grid engine lists a boid up to 8 times in "
+                                      "its own cell (overlap cell == own cell); use the all-pairs engine");
+        }
+    }
+    k.refG = refG;
+    k.refGS = refGS;
+    k.refR = refR;
+
+    // device binning grid: cells of side >= 1.01 * filter radius, capped
+    int G = 0;
+    if (p.engine == BOIDS_ENGINE_GRID && rf > 0) {
+        double g = std::floor(p.field_size / (rf * 1.01));
+        const double cap = std::cbrt(std::fmax(2.0 * k.n, 2097152.0));
+        if (g > cap) g = std::floor(cap);
+        G = g >= 3 ? (int)g : 0;  // fewer than 3 cells per axis: scan all pairs
+    }
+    k.G = G;
+    k.inv_side = G ? (float)(G / p.field_size) : 0.f;
+    s->engine = G ? 1 : 0;
+
+    int rc = 0;
+    if ((rc = use_device(s))) { delete s; return rc; }
+    DevBuffers &b = s->b;
+    const size_t n = k.n;
+#define ALLOC(...)                          \
+    if ((rc = dalloc(__VA_ARGS__))) {       \
+        free_buffers(b);                    \
+        delete s;                           \
+        return rc;                          \
+    }
+    ALLOC(&b.pos[0], n);
+    ALLOC(&b.pos[1], n);
+    ALLOC(&b.vel[0], n);
+    ALLOC(&b.vel[1], n);
+    ALLOC(&b.stage, 6 * n);
+    if (s->engine == 1) {
+        b.ncell = (uint32_t)G * G * G;
+        b.ncell_pad = (b.ncell + 1 + boidsgpu::kScanTile - 1) / boidsgpu::kScanTile * boidsgpu::kScanTile;
+        b.nscan_blocks = b.ncell_pad / boidsgpu::kScanTile;
+        ALLOC(&b.key, n);
+        ALLOC(&b.rank, n);
+        ALLOC(&b.count, b.ncell_pad, true);
+        ALLOC(&b.lstart, b.ncell_pad);
+        ALLOC(&b.bsum, b.nscan_blocks);
+        ALLOC(&b.ticket, 1, true);
+        const size_t ndense = std::min<size_t>(b.ncell, n / boidsgpu::kDenseMin) + 1;
+        ALLOC(&b.dense_list, ndense);
+        ALLOC(&b.dense_n, 1, true);
+        int nsm = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p.device);
+        b.dense_grid = (uint32_t)std::max(1, nsm) * 8;
+    } else {
+        b.ap_cap = boidsgpu::kApCap;
+        ALLOC(&b.ap_cnt, n, true);
+        ALLOC(&b.ap_list, n * b.ap_cap);
+    }
+    if (p.flags & BOIDS_FLAG_RECORD_FORCES) ALLOC(&b.forces, 9 * n);
+#undef ALLOC
+    cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        free_buffers(b);
+        delete s;
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    s->stream = s->own_stream;
+    *out = s;
+    return BOIDS_OK;
+}
+
+void boids_destroy(boids_sim *s)
+{
+    if (!s) return;
+    cudaSetDevice(s->p.device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    free_buffers(s->b);
+    resolve_events(s);
+    for (cudaEvent_t e : s->pool) cudaEventDestroy(e);
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+    delete s;
+}
+
+int boids_set_state(boids_sim *s, const float *pos3n, const float *vel3n)
+{
+    if (!s || (!pos3n && s->k.n) || (!vel3n && s->k.n)) return fail(BOIDS_EINVAL, "boids_set_state: null argument");
+    int rc = use_device(s);
+    if (rc) return rc;
+    const uint32_t n = s->k.n;
+    if (s->engine == 1 || s->p.engine == BOIDS_ENGINE_GRID) {
+        for (size_t i = 0; i < (size_t)3 * n; ++i) {
+            const float x = pos3n[i];
+            if (!(x >= 0.0f && x <= s->k.Ff && (double)x <= s->k.F * (1.0 + 1e-6)))
+                return fail(BOIDS_EINVAL, "grid engine: positions must lie in [0, field_size]");
+        }
+    }
+    PhaseTimer t(s, 2);
+    float *dpos = s->b.stage, *dvel = s->b.stage + (size_t)3 * n;
+    CK(cudaMemcpyAsync(dpos, pos3n, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(dvel, vel3n, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s->stream));
+    s->cur = 0;
+    CK(boidsgpu::launch_pack(dpos, dvel, s->b.pos[0], s->b.vel[0], n, s->stream, &s->launches));
+    if (s->engine == 1 && (rc = grid_bin_fresh(s))) return rc;
+    s->has_state = true;
+    s->forces_valid = false;
+    return BOIDS_OK;
+}
+
+int boids_init_ex(boids_sim *s, const char *init, int32_t seed, int32_t seed_mode)
+{
+    if (!s || !init) return fail(BOIDS_EINVAL, "boids_init: null argument");
+    const uint32_t n = s->k.n;
+    const double F = s->p.field_size;
+    std::vector<float> pos((size_t)3 * n), vel((size_t)3 * n);
+    const std::string kind(init);
+    if (kind == "test" || kind == "random_uniform") {
+        const bool seeded = seed_mode < 0 ? s->p.engine == BOIDS_ENGINE_GRID : seed_mode != 0;
+        Drand48 d;
+        if (seeded) d.seed((long)seed);
+        const double vmax = s->p.velocity_max, vmin = s->p.velocity_min;
+        for (uint32_t i = 0; i < n; ++i) {
+            float *x = &pos[(size_t)3 * i], *v = &vel[(size_t)3 * i];
+            if (kind == "test") {  // src/boid_simulation_grid.cpp:100-108
+                x[0] = (float)(F * 3 / 8 + d.next() * F / 4);
+                x[1] = (float)(F * 3 / 8 + d.next() * F / 4);
+                if (d.next() > 0.5) x[2] = (float)(d.next() * F / 4 + F * 3 / 4);
+                else x[2] = (float)(d.next() * F / 4);
+            } else {  // src/boid_simulation_grid.cpp:123-126
+                x[0] = (float)(F * d.next());
+                x[1] = (float)(F * d.next());
+                x[2] = (float)(F * d.next());
+            }
+            // src/boid_simulation_grid.cpp:127-132
+            const double sp = d.next() * (vmax - vmin) + vmin;
+            const double th1 = d.next() * M_PI;
+            const double th2 = d.next() * 2.0 * M_PI;
+            v[0] = (float)(sp * std::sin(th1) * std::cos(th2));
+            v[1] = (float)(sp * std::sin(th1) * std::sin(th2));
+            v[2] = (float)(sp * std::cos(th1));
+        }
+    } else {
+        // raw float32 x,y,z,vx,vy,vz per boid (src/boid_simulation.cpp:113-136)
+        std::ifstream f(kind, std::ios::binary);
+        if (!f) return fail(BOIDS_EIO, "Invalid initial placement type or file name: " + kind);
+        std::vector<float> raw((size_t)6 * n);
+        f.read(reinterpret_cast<char *>(raw.data()), (std::streamsize)(sizeof(float) * raw.size()));
+        if ((size_t)f.gcount() != sizeof(float) * raw.size())
+            return fail(BOIDS_EIO, "initialization file holds fewer than number_of_agents boids: " + kind);
+        for (uint32_t i = 0; i < n; ++i) {
+            for (int c = 0; c < 3; ++c) {
+                pos[(size_t)3 * i + c] = raw[(size_t)6 * i + c];
+                vel[(size_t)3 * i + c] = raw[(size_t)6 * i + 3 + c];
+            }
+        }
+    }
+    int rc = boids_set_state(s, pos.data(), vel.data());
+    if (rc) return rc;
+    return boids_synchronize(s);  // the host vectors die here
+}
+
+int boids_init(boids_sim *s, const char *init, int32_t seed) { return boids_init_ex(s, init, seed, -1); }
+
+int boids_step(boids_sim *s, int32_t steps)
+{
+    if (!s || steps < 0) return fail(BOIDS_EINVAL, "boids_step: bad argument");
+    if (!s->has_state) return fail(BOIDS_ESTATE, "boids_step: no state (call boids_init or boids_set_state)");
+    int rc = use_device(s);
+    if (rc) return rc;
+    const bool rec = s->b.forces != nullptr;
+    for (int32_t t = 0; t < steps; ++t) {
+        if (s->engine == 1) {
+            {
+                PhaseTimer pt(s, 0);
+                CK(boidsgpu::launch_grid_scan(s->b, s->stream, &s->launches));
+                CK(boidsgpu::launch_grid_scatter(s->k, s->b, s->cur, true, s->stream, &s->launches));
+                s->acc.bin_launches += 2;
+            }
+            PhaseTimer pt(s, 1);
+            CK(boidsgpu::launch_grid_force(s->k, s->b, 1 - s->cur, false, rec, s->stream, &s->launches));
+            s->acc.force_launches += 1;
+        } else {
+            PhaseTimer pt(s, 1);
+            CK(boidsgpu::launch_allpairs(s->k, s->b, s->cur, false, rec, s->stream, &s->launches));
+            s->cur = 1 - s->cur;
+            s->acc.force_launches += 2;
+        }
+        s->acc.steps++;
+        s->steps_done++;
+    }
+    if (steps > 0) s->forces_valid = rec;
+    return BOIDS_OK;
+}
+
+int boids_get_state(boids_sim *s, float *pos3n, float *vel3n)
+{
+    if (!s) return fail(BOIDS_EINVAL, "boids_get_state: null handle");
+    if (!s->has_state) return fail(BOIDS_ESTATE, "boids_get_state: no state");
+    int rc = use_device(s);
+    if (rc) return rc;
+    const uint32_t n = s->k.n;
+    float *dpos = s->b.stage, *dvel = s->b.stage + (size_t)3 * n;
+    {
+        PhaseTimer t(s, 2);
+        CK(boidsgpu::launch_unpack(s->b.pos[s->cur], s->b.vel[s->cur], pos3n ? dpos : nullptr,
+                                   vel3n ? dvel : nullptr, n, s->stream, &s->launches));
+        if (pos3n) CK(cudaMemcpyAsync(pos3n, dpos, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s->stream));
+        if (vel3n) CK(cudaMemcpyAsync(vel3n, dvel, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s->stream));
+    }
+    return boids_synchronize(s);
+}
+
+int boids_get_forces(boids_sim *s, float *force9n)
+{
+    if (!s || !force9n) return fail(BOIDS_EINVAL, "boids_get_forces: null argument");
+    if (!s->b.forces) return fail(BOIDS_ESTATE, "boids_get_forces: handle created without BOIDS_FLAG_RECORD_FORCES");
+    if (!s->forces_valid) return fail(BOIDS_ESTATE, "boids_get_forces: no step since the state was set");
+    int rc = use_device(s);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(force9n, s->b.forces, sizeof(float) * 9 * s->k.n, cudaMemcpyDeviceToHost, s->stream));
+    return boids_synchronize(s);
+}
+
+int boids_get_cells(boids_sim *s, int32_t *gi8)
+{
+    if (!s || !gi8) return fail(BOIDS_EINVAL, "boids_get_cells: null argument");
+    if (!s->ref_geometry_ok) return fail(BOIDS_EINVAL, "boids_get_cells: geometry has no valid reference grid");
+    if (!s->has_state) return fail(BOIDS_ESTATE, "boids_get_cells: no state");
+    int rc = use_device(s);
+    if (rc) return rc;
+    if (!s->b.cells8 && (rc = dalloc(&s->b.cells8, (size_t)8 * s->k.n))) return rc;
+    CK(boidsgpu::launch_ref_cells(s->k, s->b.pos[s->cur], s->b.cells8, s->stream, &s->launches));
+    CK(cudaMemcpyAsync(gi8, s->b.cells8, sizeof(int32_t) * 8 * s->k.n, cudaMemcpyDeviceToHost, s->stream));
+    return boids_synchronize(s);
+}
+
+int boids_get_neighbor_sets(boids_sim *s, int32_t *count3n, uint64_t *hash3n)
+{
+    if (!s || !count3n || !hash3n) return fail(BOIDS_EINVAL, "boids_get_neighbor_sets: null argument");
+    if (!s->has_state) return fail(BOIDS_ESTATE, "boids_get_neighbor_sets: no state");
+    int rc = use_device(s);
+    if (rc) return rc;
+    const size_t n = s->k.n;
+    if (!s->b.dcnt && (rc = dalloc(&s->b.dcnt, 3 * n))) return rc;
+    if (!s->b.dhash && (rc = dalloc(&s->b.dhash, 3 * n))) return rc;
+    if (s->engine == 1) {
+        CK(boidsgpu::launch_grid_scan(s->b, s->stream, &s->launches));
+        CK(boidsgpu::launch_grid_scatter(s->k, s->b, s->cur, false, s->stream, &s->launches));
+        CK(boidsgpu::launch_grid_force(s->k, s->b, 1 - s->cur, true, false, s->stream, &s->launches));
+    } else {
+        CK(boidsgpu::launch_allpairs(s->k, s->b, s->cur, true, false, s->stream, &s->launches));
+    }
+    CK(cudaMemcpyAsync(count3n, s->b.dcnt, sizeof(int32_t) * 3 * n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(hash3n, s->b.dhash, sizeof(uint64_t) * 3 * n, cudaMemcpyDeviceToHost, s->stream));
+    return boids_synchronize(s);
+}
+
+int boids_get_grid_info(boids_sim *s, boids_grid_info *info)
+{
+    if (!s || !info) return fail(BOIDS_EINVAL, "boids_get_grid_info: null argument");
+    info->ref_interaction_range = s->k.refR;
+    info->ref_grid_num = s->ref_geometry_ok ? s->k.refG : 0;
+    info->ref_grid_size = s->k.refGS;
+    info->dev_cells_per_axis = s->k.G;
+    info->dev_cell_size = s->k.G ? (float)(s->p.field_size / s->k.G) : 0.f;
+    info->list_capacity = s->engine == 1 ? boidsgpu::kListCap : boidsgpu::kApCap;
+    return BOIDS_OK;
+}
+
+int boids_set_stream(boids_sim *s, void *stream)
+{
+    if (!s) return fail(BOIDS_EINVAL, "boids_set_stream: null handle");
+    int rc = use_device(s);
+    if (rc) return rc;
+    // order the switch: work queued on the old stream completes first
+    CK(cudaStreamSynchronize(s->stream));
+    s->stream = stream ? static_cast<cudaStream_t>(stream) : s->own_stream;
+    return BOIDS_OK;
+}
+
+int boids_synchronize(boids_sim *s)
+{
+    if (!s) return fail(BOIDS_EINVAL, "boids_synchronize: null handle");
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaGetLastError());
+    return BOIDS_OK;
+}
+
+int boids_profile_enable(boids_sim *s, int32_t on)
+{
+    if (!s) return fail(BOIDS_EINVAL, "boids_profile_enable: null handle");
+    s->prof = on != 0;
+    return BOIDS_OK;
+}
+
+int boids_profile_read(boids_sim *s, boids_profile_t *out, int32_t reset)
+{
+    if (!s || !out) return fail(BOIDS_EINVAL, "boids_profile_read: null argument");
+    int rc = use_device(s);
+    if (rc) return rc;
+    resolve_events(s);
+    *out = s->acc;
+    if (reset) s->acc = boids_profile_t{};
+    return BOIDS_OK;
+}
+
+uint64_t boids_kernel_launches(boids_sim *s) { return s ? s->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,104 @@
+// boids_engine.h -- constants and kernel launchers shared by the C-ABI host
+// code (boids_capi.cpp, compiled by g++) and the kernels (boids_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "boids_softfp.h"
+
+namespace boidsgpu {
+
+// Every comparison of the reference that mixes a float with a double is
+// replaced by an exactly equivalent float comparison against a constant the
+// host derives once:
+//   (double)f <  d   <=>  f <  up(d)      (up: smallest float >= d)
+//   (double)f >  d   <=>  f >  dn(d)      (dn: largest float  <= d)
+// The radius test of Boid::isInsideArea (src/boid.cpp:28),
+// (double)sqrtf(d2) < r, becomes d2 < d2_lim with d2_lim the smallest float
+// whose correctly rounded square root reaches r; the view-cone test
+// acos(c) <= pi*a (src/boid.cpp:34-35) becomes cstar <= c <= 1, with cstar
+// found on the host with the same acosf the reference calls.
+struct RuleConst {
+    float d2_lim;     // radius test: d2 < d2_lim
+    float cstar;      // smallest c with (double)acosf(c) <= M_PI*sight_angle
+    int32_t all_round;  // sight_angle >= 1.0: the cone test is skipped
+    int32_t pad;
+};
+
+enum { RULE_COH = 0, RULE_SEP = 1, RULE_ALI = 2 };
+
+struct StepConst {
+    uint32_t n;          // boids
+    int32_t G;           // device cells per axis (>= 3), 0 for all-pairs
+    double F;            // field size (host side only)
+    SoftDouble Fsd;      // the field size in integer form, for exact float +- double
+    float Ff;            // (float)F, for approximate filters
+    float F_dn;          // dn(F): wrap test x > F
+    float halfF_dn;      // dn(F/2): minimum-image tests
+    float inv_side;      // cells per unit length of the device grid
+    float filt_r2;       // squared radius of the conservative fast filter
+    float box_lim;       // all-pairs box filter: ||dx| - F/2| > box_lim
+    float halfFf;        // (float)(F/2) for the box filter
+    float cc, cs, ca;    // (float) force coefficients: cohesion, separation, alignment
+    float vmax_dn, vmin_up;  // speed clamp tests
+    float vmax_f, vmin_f;    // speed clamp scale factors (float)vmax, (float)vmin
+    float d2_any;        // largest d2_lim of the three rules
+    float cone_band;     // approximate cone tests closer than this to a threshold are redone exactly
+    int32_t id_bits;     // bits needed for the largest boid id, rounded up to a multiple of 4
+    RuleConst rule[3];   // cohesion, separation, alignment
+    // the reference's overlapping grid, for Boid::grid_index parity
+    int32_t refG;
+    float refGS, refR;
+};
+
+// Device scratch of one engine handle.  Sizes in elements.
+struct DevBuffers {
+    float4 *pos[2], *vel[2];   // ping-pong state, float4 (w of pos = id bits)
+    uint32_t *key, *rank;      // per slot: device cell and rank inside it
+    uint32_t *count;           // per cell (padded): boids binned so far
+    uint32_t *lstart;          // per cell (padded): exclusive scan inside a tile
+    uint32_t *bsum;            // per scan tile: offset of the tile
+    uint32_t *ticket;          // scan completion counter (1 word)
+    uint32_t *ap_cnt, *ap_list;  // all-pairs: per boid neighbour count and list
+    float *forces;             // 9 per boid (id order), optional
+    float *stage;              // 6 per boid, host<->device staging
+    int32_t *cells8;           // 8 per boid (id order)
+    int32_t *dcnt;             // 3 per boid (id order)
+    uint64_t *dhash;           // 3 per boid (id order)
+    uint32_t *dense_list;      // cells holding >= kDenseMin boids, this step
+    uint32_t *dense_n;         // their number (1 word)
+    uint32_t ncell, ncell_pad, nscan_blocks;
+    uint32_t dense_grid;       // CTAs of the dense-cell kernel
+    uint32_t ap_cap;
+};
+
+constexpr int kScanTile = 2048;       // cells per scan block (256 threads x 8)
+constexpr int kListCap = 32;          // grid engine, sparse cells: sorted neighbours kept per pass
+constexpr int kDenseMin = 12;         // boids in a cell for the CTA-per-cell path
+constexpr int kDenseCap = 2048;       // candidates of a dense cell held in shared memory
+constexpr int kCandDefer = 192;       // a sparse cell with more candidates joins the dense path
+constexpr int kApCap = 64;            // all-pairs engine: neighbours kept per boid
+constexpr uint32_t kMaxBoids = 1u << 29;  // slot index packs into 29 bits
+
+// Launchers.  Each returns the launch's cudaError_t and adds the number of
+// kernels it launched to *launches.
+cudaError_t launch_pack(const float *pos3, const float *vel3, float4 *pos4, float4 *vel4,
+                        uint32_t n, cudaStream_t s, uint64_t *launches);
+cudaError_t launch_unpack(const float4 *pos4, const float4 *vel4, float *pos3, float *vel3,
+                          uint32_t n, cudaStream_t s, uint64_t *launches);
+cudaError_t launch_grid_keys(const StepConst &k, const float4 *pos, uint32_t *key, uint32_t *rank,
+                             uint32_t *count, cudaStream_t s, uint64_t *launches);
+cudaError_t launch_grid_scan(const DevBuffers &b, cudaStream_t s, uint64_t *launches);
+cudaError_t launch_grid_scatter(const StepConst &k, const DevBuffers &b, int from, bool zero_counts,
+                                cudaStream_t s, uint64_t *launches);
+// Rules + integration over the sorted state b.pos[from]; writes the new state
+// to b.pos[1-from] (diag == false) or neighbour-set fingerprints (diag == true).
+cudaError_t launch_grid_force(const StepConst &k, const DevBuffers &b, int from, bool diag,
+                              bool record_forces, cudaStream_t s, uint64_t *launches);
+cudaError_t launch_allpairs(const StepConst &k, const DevBuffers &b, int from, bool diag,
+                            bool record_forces, cudaStream_t s, uint64_t *launches);
+cudaError_t launch_ref_cells(const StepConst &k, const float4 *pos, int32_t *cells8, cudaStream_t s,
+                             uint64_t *launches);
+
+}  // namespace boidsgpu

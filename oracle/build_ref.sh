@@ -1,0 +1,26 @@
+#!/usr/bin/env bash
+# Builds the reference engine from its own sources into oracle/_ref/ (test
+# infrastructure only).  Only the four engine sources are compiled; the CLI
+# (src/main.cpp, src/args.cpp) needs Boost, which is absent, and is not built.
+# Flags follow the reference's CMakeLists.txt (-std=c++11 -O3, OpenMP) plus
+# -ffp-contract=off so that an aarch64 host rounds like the x86 build.
+#
+# usage: oracle/build_ref.sh [REFERENCE_SRC_DIR]   (default /root/reference/src)
+set -euo pipefail
+here="$(cd "$(dirname "$0")" && pwd)"
+src="${1:-${REF_SRC:-/root/reference/src}}"
+out="$here/_ref"
+if [ ! -f "$src/boid_simulation_grid.cpp" ]; then
+    echo "build_ref.sh: reference sources not found at $src" >&2
+    exit 3
+fi
+mkdir -p "$out"
+flags="-std=c++11 -O3 -fopenmp -ffp-contract=off -fPIC -shared -w"
+g++ $flags -DREF_GRID -I"$src" "$here/ref_driver.cpp" \
+    "$src/boid_simulation_grid.cpp" "$src/boid.cpp" "$src/vector3D.cpp" \
+    -o "$out/libref_grid.so" &
+g++ $flags -I"$src" "$here/ref_driver.cpp" \
+    "$src/boid_simulation.cpp" "$src/boid.cpp" "$src/vector3D.cpp" \
+    -o "$out/libref_allpairs.so" &
+wait %1 && wait %2
+echo "built $out/libref_grid.so $out/libref_allpairs.so"

@@ -1,0 +1,250 @@
+"""GPU parity: the CUDA engines against the oracle, through the C ABI.
+
+The bar is bit-for-bit equality with the reference's FP32 arithmetic (the
+oracle restates it and is itself pinned bit-for-bit to the reference engine
+compiled from its sources, see test_oracle.py).  Trajectories are compared
+bit-for-bit over the step counts of the reference's own test scripts
+(test/compare_grid.sh: N=100 T=30, test/compare_legacy.sh: N=1000 T=30).
+"""
+import numpy as np
+import pytest
+
+from conftest import assert_bits_equal, make_params, make_sim
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    # name, n, field, settings, init, steps
+    ("compare_grid_sh", 100, 1.0, "TEST_INI", "test", 30),
+    ("compare_legacy_sh", 1000, 1.0, "TEST_INI", "test", 30),
+    ("marun2019_F0.5", 2048, 0.5, "MARUN2019", "random_uniform", 50),
+    ("marun2019_config0", 16384, 1.0, "MARUN2019", "random_uniform", 10),
+]
+
+
+def _oracle_run(O, p, engine, pos, vel, steps):
+    pos, vel = pos.copy(), vel.copy()
+    if engine == "grid":
+        f = O.GridPort(p, pos).step(pos, vel, steps, forces=True)
+    else:
+        f = O.step_allpairs(p, pos, vel, steps, forces=True)
+    return pos, vel, f
+
+
+@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_trajectory_bit_exact(boids_lib, oracle_mod, engine, case):
+    name, n, field, sname, init, steps = case
+    O = oracle_mod
+    prm = getattr(O, sname)
+    if engine == "allpairs" and n > 4096:
+        steps = 3
+    p = make_params(O, n, field, prm)
+    sim = make_sim(boids_lib, engine, n, field, prm)
+    sim.initialization_type = init
+    sim.init()  # the engine's own seeding rule, as in the reference
+    pos0, vel0 = O.init_state(p, init, seeded=(engine == "grid"), seed=12345)
+    gp, gv = sim.state()
+    assert_bits_equal(gp, pos0, "init positions")
+    assert_bits_equal(gv, vel0, "init velocities")
+    sim.update(steps)
+    gp, gv = sim.state()
+    gf = sim.forces()
+    op, ov, of = _oracle_run(O, p, engine, pos0, vel0, steps)
+    assert_bits_equal(gp, op, "positions after %d steps" % steps)
+    assert_bits_equal(gv, ov, "velocities after %d steps" % steps)
+    assert_bits_equal(gf, of, "forces of step %d" % steps)
+
+
+@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+def test_single_step_forces_from_identical_state(boids_lib, oracle_mod, engine):
+    """The same evolved state is fed to both sides; one step's get_force must match."""
+    O = oracle_mod
+    n, field = 16384, 1.0
+    p = make_params(O, n, field, O.MARUN2019)
+    pos, vel = O.init_state(p, "random_uniform", True, 7)
+    O.GridPort(p, pos).step(pos, vel, 120)  # clustered, realistic state
+    sim = make_sim(boids_lib, engine, n, field, O.MARUN2019)
+    sim.set_state(pos, vel)
+    sim.update(1)
+    op, ov, of = _oracle_run(O, p, "grid", pos, vel, 1)
+    assert_bits_equal(sim.forces(), of, "forces")
+    gp, gv = sim.state()
+    assert_bits_equal(gp, op, "positions")
+    assert_bits_equal(gv, ov, "velocities")
+
+
+def test_grid_equals_allpairs_on_gpu(boids_lib, oracle_mod):
+    O = oracle_mod
+    n, field = 8192, 0.8
+    prm = O.MARUN2019
+    p = make_params(O, n, field, prm)
+    pos, vel = O.init_state(p, "random_uniform", True, 99)
+    a = make_sim(boids_lib, "grid", n, field, prm)
+    b = make_sim(boids_lib, "allpairs", n, field, prm)
+    a.set_state(pos, vel)
+    b.set_state(pos, vel)
+    a.update(20)
+    b.update(20)
+    ap, av = a.state()
+    bp, bv = b.state()
+    assert_bits_equal(ap, bp, "positions")
+    assert_bits_equal(av, bv, "velocities")
+
+
+def test_reference_cells_bit_exact(boids_lib, oracle_mod):
+    """Boid::grid_index (primary + overlapped cells) equals the reference's."""
+    O = oracle_mod
+    n, field = 65536, 1.6
+    p = make_params(O, n, field, O.MARUN2019)
+    pos, vel = O.init_state(p, "random_uniform", True, 12345)
+    sim = make_sim(boids_lib, "grid", n, field, O.MARUN2019)
+    sim.set_state(pos, vel)
+    sim.update(5)
+    gp, gv = sim.state()
+    cells = sim.cells()
+    ref = O.ref_cells(p, gp.reshape(-1))
+    assert np.array_equal(cells, ref)
+    info = sim.grid_info()
+    assert info["ref_grid_num"] == 15
+    assert O.grid_geometry(p)[1] == 15
+
+
+@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+def test_neighbor_sets_bit_exact(boids_lib, oracle_mod, engine):
+    O = oracle_mod
+    n, field = 32768, 1.27
+    p = make_params(O, n, field, O.MARUN2019)
+    pos, vel = O.init_state(p, "random_uniform", True, 3)
+    O.GridPort(p, pos).step(pos, vel, 60)
+    sim = make_sim(boids_lib, engine, n, field, O.MARUN2019)
+    sim.set_state(pos, vel)
+    c, h = sim.neighbor_sets()
+    oc, oh = O.neighbor_sets(p, pos, vel)
+    assert np.array_equal(c, oc)
+    assert np.array_equal(h, oh)
+    # the diagnostic does not advance or disturb the state
+    gp, gv = sim.state()
+    assert_bits_equal(gp, pos, "state after diagnostics")
+    sim.update(1)
+    op, ov, of = _oracle_run(O, p, "grid", pos, vel, 1)
+    assert_bits_equal(sim.state()[0], op, "step after diagnostics")
+
+
+@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+def test_dense_cluster_overflow_paths(boids_lib, oracle_mod, engine):
+    """Hundreds of neighbours per boid: more than the per-thread list holds
+    (grid: several sorted passes; all-pairs: ordered full scan)."""
+    O = oracle_mod
+    rng = np.random.default_rng(5)
+    n, field = 600, 1.0
+    prm = O.MARUN2019
+    p = make_params(O, n, field, prm)
+    pos = (0.5 + 0.02 * rng.standard_normal((n, 3))).astype(np.float32).reshape(-1)
+    pos[: 3 * 50] = rng.random(3 * 50, dtype=np.float32)  # some isolated boids
+    vel = (0.003 * rng.standard_normal((n, 3))).astype(np.float32).reshape(-1)
+    sim = make_sim(boids_lib, engine, n, field, prm)
+    sim.set_state(pos, vel)
+    sim.update(3)
+    op, ov, of = _oracle_run(O, p, "allpairs", pos, vel, 3)
+    gp, gv = sim.state()
+    assert_bits_equal(gp, op, "positions")
+    assert_bits_equal(gv, ov, "velocities")
+    assert_bits_equal(sim.forces(), of, "forces")
+
+
+@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+def test_degenerate_pairs(boids_lib, oracle_mod, engine):
+    """Coincident boids (distance 0), zero velocities (0/0 in the cone test),
+    boids on the periodic faces and at x == field_size exactly."""
+    O = oracle_mod
+    n, field = 64, 1.0
+    prm = dict(O.MARUN2019)
+    p = make_params(O, n, field, prm)
+    rng = np.random.default_rng(11)
+    pos = rng.random((n, 3), dtype=np.float32)
+    vel = (0.004 * rng.standard_normal((n, 3))).astype(np.float32)
+    pos[1] = pos[0]                      # coincident
+    vel[2] = 0.0                         # no heading
+    pos[3] = [0.0, 0.5, 0.5]; pos[4] = [np.float32(field), 0.5, 0.5]  # across x faces
+    pos[5] = [0.999, 0.001, 0.0]; pos[6] = [0.001, 0.999, 0.9995]
+    pos[7] = [0.5, 0.0, np.float32(field)]
+    vel[3] = [-0.004, 0, 0]
+    sim = make_sim(boids_lib, engine, n, field, prm)
+    sim.set_state(pos, vel)
+    sim.update(4)
+    op, ov, of = _oracle_run(O, p, "allpairs", pos.reshape(-1), vel.reshape(-1), 4)
+    gp, gv = sim.state()
+    assert_bits_equal(gp, op, "positions")
+    assert_bits_equal(gv, ov, "velocities")
+    assert_bits_equal(sim.forces(), of, "forces")
+
+
+def test_all_round_angles_and_test_ini(boids_lib, oracle_mod):
+    """Sight angles >= 1 skip the cone test entirely (src/boid.cpp:29-31)."""
+    O = oracle_mod
+    prm = dict(sep=(0.02, 1.0, 0.001), ali=(0.05, 1.5, 0.05), coh=(0.05, 0.2, 0.01),
+               vmax=0.004, vmin=0.0005)
+    n, field = 4096, 0.6
+    p = make_params(O, n, field, prm)
+    pos, vel = O.init_state(p, "random_uniform", True, 1)
+    for engine in ("grid", "allpairs"):
+        sim = make_sim(boids_lib, engine, n, field, prm)
+        sim.set_state(pos, vel)
+        sim.update(10)
+        op, ov, of = _oracle_run(O, p, "allpairs", pos, vel, 10)
+        assert_bits_equal(sim.state()[0], op, engine)
+        assert_bits_equal(sim.forces(), of, engine)
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 33])
+def test_tiny_populations(boids_lib, oracle_mod, n):
+    O = oracle_mod
+    for engine in ("grid", "allpairs"):
+        p = make_params(O, n, 1.0, O.MARUN2019)
+        sim = make_sim(boids_lib, engine, n, 1.0, O.MARUN2019)
+        sim.init()
+        pos, vel = O.init_state(p, "random_uniform", engine == "grid", 12345)
+        sim.update(5)
+        op, ov, of = _oracle_run(O, p, "allpairs", pos, vel, 5)
+        gp, gv = sim.state()
+        assert_bits_equal(gp, op, "positions")
+        assert_bits_equal(gv, ov, "velocities")
+
+
+def test_fp64_oracle_tolerance(boids_lib, oracle_mod):
+    """Per-rule force error of the FP32 step against the FP64 restatement.
+
+    Tolerance, written here: for each rule the aggregate (Frobenius) relative
+    error over all boids is <= 1e-5, and every boid's error is <= 1e-4 of the
+    rule's operand scale (cohesion: c*max(|x_i|, |mean x_j|); separation:
+    c*n_sep; alignment: c*max(|v_i|, |mean v_j|)).  The per-boid plain
+    relative error can exceed 1e-5 for cohesion: the reference forms
+    mean(x_j) - x_i in float, which cancels; the GPU is bit-identical to the
+    reference, so it inherits exactly that error.
+    """
+    O = oracle_mod
+    n, field = 65536, 1.6
+    prm = O.MARUN2019
+    p = make_params(O, n, field, prm)
+    pos, vel = O.init_state(p, "random_uniform", True, 12345)
+    O.GridPort(p, pos).step(pos, vel, 50)
+    sim = make_sim(boids_lib, "grid", n, field, prm)
+    sim.set_state(pos, vel)
+    sim.update(1)
+    f32 = sim.forces().astype(np.float64)
+    f64 = O.forces_f64(p, pos, vel)
+    cnt, _ = O.neighbor_sets(p, pos, vel)
+    P = pos.reshape(n, 3).astype(np.float64)
+    V = vel.reshape(n, 3).astype(np.float64)
+    cc, cs, ca = prm["coh"][2], prm["sep"][2], prm["ali"][2]
+    scale = [cc * np.maximum(np.linalg.norm(P, axis=1), np.linalg.norm(f64[:, 0:3] / cc + P, axis=1)),
+             cs * cnt[:, 1],
+             ca * np.maximum(np.linalg.norm(V, axis=1), np.linalg.norm(f64[:, 6:9] / ca + V, axis=1))]
+    for r in range(3):
+        a, b = f32[:, 3 * r:3 * r + 3], f64[:, 3 * r:3 * r + 3]
+        assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b) + 1e-30
+        err = np.linalg.norm(a - b, axis=1)
+        s = scale[r]
+        assert np.all(err[s == 0] == 0)
+        assert np.all(err[s > 0] <= 1e-4 * s[s > 0])
