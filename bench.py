@@ -1,0 +1,365 @@
+#!/usr/bin/env python3
+"""Benchmark: boid-steps/s of the per-timestep update at N=2^20 (grid, FP32).
+
+Workload (BoidsSimulatorMPI's uniform-grid configuration): N = 2^20 boids in a
+periodic cube of side F = 4.0 (the number density of 16384 boids per unit
+volume), rule radii, view angles, weights and speed limits of
+settings/marun2019.ini, dt = 1, initial state "random_uniform" drawn with
+srand48(12345) exactly as the reference draws it.  One bench step = one
+BoidSimulation::update() of all N boids.  Synthetic data: the state is
+generated, no dataset is involved.
+
+Our arm (--impl ours): the CUDA grid engine through its C ABI.  Before every
+timed step a 256 MiB buffer is written to flush L2 (outside the timed
+events); each step is timed with CUDA events on the engine's stream.  `e2e`
+times the same steps through the C ABI with host buffers: every step uploads
+the state from pinned host memory, updates, and downloads the new state.
+
+Reference arm (--impl reference): the reference's own CPU engine
+(src/boid_simulation_grid.cpp, built from its sources into oracle/_ref) when
+it is present, else the oracle's C port of it, on all host cores, same
+workload; each step is one update() of all N boids.
+
+Multi-GPU (torchrun, N > 1): independent replicas, one per GPU, each with its
+own seed; value = boid-steps of all ranks / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "boid-steps/s at N=2^20 (grid, FP32)"
+UNIT = "boid-steps/s"
+MARUN2019 = dict(sep=(0.01, 0.5, 0.002), ali=(0.05, 0.3333333333333333, 0.06),
+                 coh=(0.05, 0.5, 0.008), vmax=0.005, vmin=0.001)
+# algorithmic bytes per boid and step (state read + written once per pass)
+RULE_BYTES = 72    # rule kernels: read pos+vel (32), write pos+vel (32), key+rank (8)
+STEP_BYTES = 144   # whole step: rule kernels + scan/scatter (64 + 8)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--field", type=float, default=4.0)
+    ap.add_argument("--seed", type=int, default=12345)
+    ap.add_argument("--engine", choices=["grid", "allpairs"], default="grid")
+    ap.add_argument("--late-presteps", type=int, default=1000,
+                    help="untimed steps before the supplementary clustered-regime timing (0: skip)")
+    ap.add_argument("--cpu-sample-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(a):
+    return {"workload": "boids grid update, N=%d, F=%g, marun2019.ini, random_uniform seed %d"
+                        % (a.n, a.field, a.seed),
+            "n": a.n, "field_size": a.field, "settings": "marun2019.ini", "dt": 1,
+            "init": "random_uniform", "seed": a.seed, "engine": a.engine,
+            "state": "timed from the initial state, after the warm-up steps"}
+
+
+def dist_setup(a):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if a.impl == "ours" else "gloo"
+        dist.init_process_group(backend)
+        return dist.get_rank(), ws, dist
+    return 0, 1, None
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ reference arm
+
+def run_reference(a):
+    import numpy as np
+    import oracle as O
+    rank, ws, dist = dist_setup(a)
+    if rank != 0:
+        return
+    O.build()
+    p = O.params(a.n, a.field, MARUN2019["sep"], MARUN2019["ali"], MARUN2019["coh"],
+                 MARUN2019["vmax"], MARUN2019["vmin"])
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    if O.ref_available("grid"):
+        kind = "reference"
+        eng = O.RefEngine("grid", p, "random_uniform", a.seed)
+        eng.init()
+        step = eng.update
+        sample = "src/boid_simulation_grid.cpp built from its sources (oracle/_ref), update() of all N"
+    else:
+        kind = "port"
+        pos, vel = O.init_state(p, "random_uniform", True, a.seed)
+        g = O.GridPort(p, pos)
+        step = lambda k=1: g.step(pos, vel, k, threads=cores)
+        sample = "oracle C port of src/boid_simulation_grid.cpp (rules in parallel, " \
+                 "integration and rebinning serial as in the reference), update() of all N"
+    for _ in range(a.warmup):
+        step(1)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        step(1)
+    dt = time.perf_counter() - t0
+    value = a.n * a.steps / dt
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": dt * 1e3 / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": workload(a), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ our arm
+
+def cpu_baseline_sample(a, pos, vel):
+    """The oracle port (or the reference engine) timed on this host, a few steps."""
+    import numpy as np
+    import oracle as O
+    O.build()
+    p = O.params(a.n, a.field, MARUN2019["sep"], MARUN2019["ali"], MARUN2019["coh"],
+                 MARUN2019["vmax"], MARUN2019["vmin"])
+    cores = os.cpu_count() or 1
+    k = max(1, a.cpu_sample_steps)
+    pos, vel = pos.copy(), vel.copy()
+    if O.ref_available("grid"):
+        eng = O.RefEngine("grid", p, "random_uniform", a.seed)
+        eng.set_state(pos, vel)
+        t0 = time.perf_counter()
+        eng.update(k)
+        dt = time.perf_counter() - t0
+        kind = "reference"
+        what = "src/boid_simulation_grid.cpp from its sources"
+    else:
+        g = O.GridPort(p, pos)
+        t0 = time.perf_counter()
+        g.step(pos, vel, k, threads=cores)
+        dt = time.perf_counter() - t0
+        kind = "port"
+        what = "oracle C port of src/boid_simulation_grid.cpp"
+    return {"value": a.n * k / dt, "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": "%s, %d update() of all N=%d boids from the timed state" % (what, k, a.n)}
+
+
+def run_ours(a):
+    import numpy as np
+    import torch
+    import boidssimulatormpi_gb300 as B
+    rank, ws, dist = dist_setup(a)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    m = MARUN2019
+    sim = B.BoidSimulation(a.engine, device=local)
+    sim.setup(a.n, a.field, *m["sep"], *m["ali"], *m["coh"], m["vmax"], m["vmin"],
+              "random_uniform", a.seed + rank)
+    # one non-default stream for the engine, the L2 flush and the timing events
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    sim.set_stream(stream.cuda_stream)
+    sim.init()
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MiB > L2
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(a.warmup):
+        sim.update(1)
+    barrier()
+    pos0, vel0 = sim.state()  # the state the timed steps start from
+    # ---- device-resident timing, L2 flushed before every step
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+    sim.profile_read(True)
+    sim.profile_enable(True)
+    l0 = sim.kernel_launches()
+    barrier()
+    with ClockSampler(local) as clk:
+        for i in range(a.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            sim.update(1)
+            ends[i].record(stream)
+        barrier()
+    launches = sim.kernel_launches() - l0
+    prof = sim.profile_read(True)
+    sim.profile_enable(False)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = a.n * a.steps * ws / (total_ms / 1e3)
+
+    # ---- end to end through the C ABI with host buffers
+    hp = torch.empty(3 * a.n, dtype=torch.float32, pin_memory=True).numpy()
+    hv = torch.empty(3 * a.n, dtype=torch.float32, pin_memory=True).numpy()
+    hp[:] = pos0.reshape(-1)
+    hv[:] = vel0.reshape(-1)
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(a.steps):
+        sim.set_state(hp, hv)
+        sim.update(1)
+        sim.state(hp, hv)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": a.n * a.steps * ws / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(hp.nbytes + hv.nbytes),
+           "d2h_bytes_per_step": int(hp.nbytes + hv.nbytes)}
+
+    # ---- supplementary: the clustered regime later in the trajectory
+    late = None
+    if a.late_presteps > 0:
+        sim.set_state(pos0.reshape(-1), vel0.reshape(-1))
+        sim.update(a.late_presteps)
+        barrier()
+        ms = []
+        for i in range(a.steps):
+            flush.zero_()
+            s0 = torch.cuda.Event(enable_timing=True)
+            s1 = torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            sim.update(1)
+            s1.record(stream)
+            s1.synchronize()
+            ms.append(s0.elapsed_time(s1))
+        late = {"after_steps": a.warmup + a.late_presteps, "ms_per_step": sum(ms) / len(ms),
+                "value": a.n * len(ms) / (sum(ms) / 1e3), "unit": UNIT}
+
+    if rank != 0:
+        sim.close()
+        return
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    rules_ms = prof["force_ms"] / max(1, prof["steps"])
+    achieved = RULE_BYTES * a.n / (rules_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "rule kernels (k_grid_sparse + k_grid_dense)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_src, "traffic": None,
+                "bytes_per_boid": RULE_BYTES, "rules_ms_per_step": rules_ms,
+                "bin_ms_per_step": prof["bin_ms"] / max(1, prof["steps"]),
+                "step_frac": STEP_BYTES * a.n / (total_ms / a.steps / 1e3) / 1e9 / peak}
+    tr = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tr):
+        try:
+            with open(tr) as f:
+                t = json.load(f).get("rules_dram_bytes_per_boid")
+            if t:
+                roofline["traffic"] = t * a.n
+        except (OSError, ValueError):
+            pass
+    cpu = None
+    if not a.no_cpu_baseline and a.engine == "grid":
+        cpu = cpu_baseline_sample(a, pos0.reshape(-1), vel0.reshape(-1))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": total_ms / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": dict(workload(a), l2="flushed before every timed step (256 MiB write)",
+                           parallelism="replicas" if ws > 1 else "single GPU"),
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk.summary(), "late_regime": late,
+            "step_ms_min_max": [min(step_ms), max(step_ms)]}
+    sim.close()
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

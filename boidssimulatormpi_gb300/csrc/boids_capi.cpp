@@ -161,7 +161,7 @@ void free_buffers(DevBuffers &b)
 {
     void *ptrs[] = {b.pos[0], b.pos[1], b.vel[0], b.vel[1], b.key, b.rank, b.count, b.lstart,
                     b.bsum, b.ticket, b.ap_cnt, b.ap_list, b.forces, b.stage, b.cells8, b.dcnt, b.dhash,
-                    b.dense_list, b.dense_n};
+                    b.dense_list, b.dense_n, b.flag};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     b = DevBuffers{};
@@ -382,6 +382,7 @@ int boids_create(const boids_params *params, boids_sim **out)
     ALLOC(&b.vel[0], n);
     ALLOC(&b.vel[1], n);
     ALLOC(&b.stage, 6 * n);
+    ALLOC(&b.flag, 1, true);
     if (s->engine == 1) {
         b.ncell = (uint32_t)G * G * G;
         b.ncell_pad = (b.ncell + 1 + boidsgpu::kScanTile - 1) / boidsgpu::kScanTile * boidsgpu::kScanTile;
@@ -434,22 +435,28 @@ int boids_set_state(boids_sim *s, const float *pos3n, const float *vel3n)
     int rc = use_device(s);
     if (rc) return rc;
     const uint32_t n = s->k.n;
-    if (s->engine == 1 || s->p.engine == BOIDS_ENGINE_GRID) {
-        for (size_t i = 0; i < (size_t)3 * n; ++i) {
-            const float x = pos3n[i];
-            if (!(x >= 0.0f && x <= s->k.Ff && (double)x <= s->k.F * (1.0 + 1e-6)))
-                return fail(BOIDS_EINVAL, "grid engine: positions must lie in [0, field_size]");
-        }
-    }
-    PhaseTimer t(s, 2);
+    // the grid engine bins positions into cells: they must lie in the field
+    const bool check = s->p.engine == BOIDS_ENGINE_GRID;
     float *dpos = s->b.stage, *dvel = s->b.stage + (size_t)3 * n;
-    CK(cudaMemcpyAsync(dpos, pos3n, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s->stream));
-    CK(cudaMemcpyAsync(dvel, vel3n, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s->stream));
+    {
+        PhaseTimer t(s, 2);
+        if (check) CK(cudaMemsetAsync(s->b.flag, 0, sizeof(uint32_t), s->stream));
+        CK(cudaMemcpyAsync(dpos, pos3n, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(dvel, vel3n, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s->stream));
+        CK(boidsgpu::launch_pack(dpos, dvel, s->b.pos[0], s->b.vel[0], n, check ? s->b.flag : nullptr,
+                                 s->k.F_dn > s->k.Ff ? s->k.F_dn : s->k.Ff, s->stream, &s->launches));
+    }
+    s->has_state = false;
+    s->forces_valid = false;
+    if (check) {
+        uint32_t bad = 0;
+        CK(cudaMemcpyAsync(&bad, s->b.flag, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        if (bad) return fail(BOIDS_EINVAL, "grid engine: positions must lie in [0, field_size]");
+    }
     s->cur = 0;
-    CK(boidsgpu::launch_pack(dpos, dvel, s->b.pos[0], s->b.vel[0], n, s->stream, &s->launches));
     if (s->engine == 1 && (rc = grid_bin_fresh(s))) return rc;
     s->has_state = true;
-    s->forces_valid = false;
     return BOIDS_OK;
 }
 

@@ -68,6 +68,7 @@ struct DevBuffers {
     uint64_t *dhash;           // 3 per boid (id order)
     uint32_t *dense_list;      // cells holding >= kDenseMin boids, this step
     uint32_t *dense_n;         // their number (1 word)
+    uint32_t *flag;            // set_state range check (1 word)
     uint32_t ncell, ncell_pad, nscan_blocks;
     uint32_t dense_grid;       // CTAs of the dense-cell kernel
     uint32_t ap_cap;
@@ -84,7 +85,7 @@ constexpr uint32_t kMaxBoids = 1u << 29;  // slot index packs into 29 bits
 // Launchers.  Each returns the launch's cudaError_t and adds the number of
 // kernels it launched to *launches.
 cudaError_t launch_pack(const float *pos3, const float *vel3, float4 *pos4, float4 *vel4,
-                        uint32_t n, cudaStream_t s, uint64_t *launches);
+                        uint32_t n, uint32_t *bad, float hi, cudaStream_t s, uint64_t *launches);
 cudaError_t launch_unpack(const float4 *pos4, const float4 *vel4, float *pos3, float *vel3,
                           uint32_t n, cudaStream_t s, uint64_t *launches);
 cudaError_t launch_grid_keys(const StepConst &k, const float4 *pos, uint32_t *key, uint32_t *rank,

@@ -293,13 +293,18 @@ __device__ __forceinline__ void finish_boid(const Acc &a, float4 p4, float3 vi, 
 
 // ------------------------------------------------------------------ state packing
 
+// Packs an id-ordered state into float4 records (w of pos = id bits).  With
+// bad != null, a coordinate outside [0, hi] (or NaN) sets *bad.
 __global__ void k_pack(const float *__restrict__ pos3, const float *__restrict__ vel3,
-                       float4 *__restrict__ pos4, float4 *__restrict__ vel4, uint32_t n)
+                       float4 *__restrict__ pos4, float4 *__restrict__ vel4, uint32_t n,
+                       uint32_t *__restrict__ bad, float hi)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    pos4[i] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], __uint_as_float(i));
+    const float x = pos3[3 * i], y = pos3[3 * i + 1], z = pos3[3 * i + 2];
+    pos4[i] = make_float4(x, y, z, __uint_as_float(i));
     vel4[i] = make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.f);
+    if (bad && !(x >= 0.f && x <= hi && y >= 0.f && y <= hi && z >= 0.f && z <= hi)) *bad = 1u;
 }
 
 // Slot order -> id order (the reference's getters index by id).
@@ -878,10 +883,10 @@ __global__ void k_ref_cells(const float4 *__restrict__ pos, int32_t *__restrict_
 static inline unsigned blocks_for(uint32_t n, unsigned t) { return (n + t - 1) / t; }
 
 cudaError_t launch_pack(const float *pos3, const float *vel3, float4 *pos4, float4 *vel4, uint32_t n,
-                        cudaStream_t st, uint64_t *launches)
+                        uint32_t *bad, float hi, cudaStream_t st, uint64_t *launches)
 {
     if (n == 0) return cudaSuccess;
-    k_pack<<<blocks_for(n, 256), 256, 0, st>>>(pos3, vel3, pos4, vel4, n);
+    k_pack<<<blocks_for(n, 256), 256, 0, st>>>(pos3, vel3, pos4, vel4, n, bad, hi);
     ++*launches;
     return cudaGetLastError();
 }
