@@ -75,6 +75,7 @@ SIGNATURES = {
     "boids_profile_enable": (C.c_int, [_vp, C.c_int32]),
     "boids_profile_read": (C.c_int, [_vp, C.POINTER(Profile), C.c_int32]),
     "boids_kernel_launches": (C.c_uint64, [_vp]),
+    "boids_step_noalloc": (C.c_int, [C.POINTER(Params), _vp, _vp, _vp, _vp, _vp]),
     "boids_last_error": (C.c_char_p, []),
     "boids_version": (C.c_char_p, []),
 }

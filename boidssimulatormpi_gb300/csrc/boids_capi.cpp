@@ -660,3 +660,89 @@ int boids_profile_read(boids_sim *s, boids_profile_t *out, int32_t reset)
 uint64_t boids_kernel_launches(boids_sim *s) { return s ? s->launches : 0; }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ support for boids_step_noalloc
+
+namespace boidsgpu {
+
+// Records an error message for boids_last_error() on behalf of
+// boids_noalloc.cu.
+int set_last_error(int code, const char *msg) { return fail(code, msg); }
+
+// The step constants boids_create derives for a grid-engine handle, for the
+// allocation-free entry point, which has no handle.  Uses no heap memory on
+// success.
+int grid_constants_noalloc(const boids_params *params, StepConst *out)
+{
+    const boids_params &p = *params;
+    if (p.number_of_agents > kMaxBoids) return fail(BOIDS_EINVAL, "number_of_agents exceeds 2^29");
+    if (!(p.field_size > 0.0) || !std::isfinite(p.field_size))
+        return fail(BOIDS_EINVAL, "field_size must be positive and finite");
+    if (p.engine != BOIDS_ENGINE_GRID) return fail(BOIDS_EINVAL, "boids_step_noalloc runs the grid engine only");
+    const double radii[3] = {p.cohesion_sight_distance, p.separation_sight_distance, p.alignment_sight_distance};
+    for (double r : radii)
+        if (std::isnan(r)) return fail(BOIDS_EINVAL, "sight distance is NaN");
+    StepConst k{};
+    k.n = p.number_of_agents;
+    k.F = p.field_size;
+    k.Ff = (float)p.field_size;
+    k.F_dn = f_dn(p.field_size);
+    k.halfF_dn = f_dn(p.field_size / 2);
+    k.halfFf = (float)(p.field_size / 2);
+    k.cc = (float)p.cohesion_force_coefficient;
+    k.cs = (float)p.separation_force_coefficient;
+    k.ca = (float)p.alignment_force_coefficient;
+    k.vmax_dn = f_dn(p.velocity_max);
+    k.vmin_up = f_up(p.velocity_min);
+    k.vmax_f = (float)p.velocity_max;
+    k.vmin_f = (float)p.velocity_min;
+    k.Fsd = soft_double(p.field_size);
+    k.cone_band = 4e-6f;
+    int bits = 0;
+    while (bits < 32 && (1ull << bits) < (uint64_t)(k.n ? k.n : 1)) ++bits;
+    k.id_bits = std::max(4, (bits + 3) / 4 * 4);
+    const double ang[3] = {p.cohesion_sight_angle, p.separation_sight_angle, p.alignment_sight_angle};
+    float rmax = 0.f;
+    for (int r = 0; r < 3; ++r) {
+        RuleConst &q = k.rule[r];
+        q.d2_lim = radius_d2_limit(radii[r]);
+        q.all_round = ang[r] >= 1.0;
+        q.cstar = INFINITY;
+        if (!q.all_round) {
+            const int rc = cone_threshold(ang[r], &q.cstar);
+            if (rc) return rc;
+        }
+        k.d2_any = std::fmax(k.d2_any, q.d2_lim);
+        const float rup = f_up(radii[r]);
+        if (rup > rmax) rmax = rup;
+    }
+    const double ulpF = std::nextafter(std::fmax(k.Ff, 1.0f), INFINITY) - std::fmax(k.Ff, 1.0f);
+    const double rf = (double)rmax * (1.0 + 1e-4) + 8.0 * ulpF;
+    k.filt_r2 = (float)(rf * rf);
+    k.box_lim = (float)(p.field_size / 2 - rf * (1.0 + 1e-4) - 8.0 * ulpF);
+    float refR = 0.f, refGS = 0.f;
+    int refG = 0;
+    if (!ref_geometry(p, &refR, &refG, &refGS))
+        return fail(BOIDS_EINVAL, "Invalid GRID_NUM: the reference grid engine needs "
+                                  "field_size > 2 * max sight distance (src/boid_simulation_grid.cpp:86-89)");
+    if (refG == 1)
+        return fail(BOIDS_EINVAL, "GRID_NUM == 1: the reference grid engine lists a boid up to 8 times in "
+                                  "its own cell; use the all-pairs engine");
+    k.refG = refG;
+    k.refGS = refGS;
+    k.refR = refR;
+    int G = 0;
+    if (rf > 0) {
+        double g = std::floor(p.field_size / (rf * 1.01));
+        const double cap = std::cbrt(std::fmax(2.0 * k.n, 2097152.0));
+        if (g > cap) g = std::floor(cap);
+        G = g >= 3 ? (int)g : 0;
+    }
+    if (G == 0) return fail(BOIDS_EINVAL, "field too small for device cells: use the handle API");
+    k.G = G;
+    k.inv_side = (float)(G / p.field_size);
+    *out = k;
+    return BOIDS_OK;
+}
+
+}  // namespace boidsgpu

@@ -159,6 +159,31 @@ int boids_profile_read(boids_sim *sim, boids_profile_t *out, int32_t reset);
 /* Number of this library's kernels launched by the handle so far. */
 uint64_t boids_kernel_launches(boids_sim *sim);
 
+/* Scratch reserved by boids_step_noalloc on every GPU that loads the library. */
+#define BOIDS_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* One grid-engine update (BoidSimulation::update semantics, bit-identical to
+ * boids_step) that allocates no memory -- this entry point has no
+ * counterpart in the reference.  It is for callers that cannot let a library
+ * allocate device memory: applications that own the GPU through their own
+ * pool or a fixed budget, and latency-critical loops that must not run into
+ * cudaMalloc/cudaFree, which can synchronize the device.  Inputs and outputs
+ * are caller-owned DEVICE arrays in id order (3 floats per boid, xyz); in and
+ * out must not overlap.  params->engine must be BOIDS_ENGINE_GRID; positions
+ * must lie in [0, field_size] (not checked here).
+ *
+ * All scratch lives in one static device array of BOIDS_NOALLOC_SCRATCH_BYTES
+ * that every GPU loading the library holds until the process exits; a step
+ * needing more (roughly 440 000 boids at the reference's density) returns
+ * BOIDS_EINVAL.  The first call on a device looks up the array's device
+ * address, so make that first call before any stream capture.  Every call
+ * shares the array: calls whose GPU work overlaps (other streams, other
+ * threads on the same device) race; order them on one stream.  The work is
+ * queued on cuda_stream (a cudaStream_t; NULL is the legacy default stream)
+ * and the call returns without waiting for it. */
+int boids_step_noalloc(const boids_params *params, const float *pos3n_in, const float *vel3n_in,
+                       float *pos3n_out, float *vel3n_out, void *cuda_stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char *boids_last_error(void);
 
