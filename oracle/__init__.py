@@ -81,6 +81,7 @@ def lib():
         L.orc_grid_destroy.argtypes = [C.c_void_p]
         L.orc_ref_cells.argtypes = [P, _f32p, _i32p]
         L.orc_neighbor_sets.argtypes = [P, _f32p, _f32p, _i32p, _u64p, C.c_int]
+        L.orc_neighbor_sets_ex.argtypes = [P, _f32p, _f32p, _i32p, _u64p, C.c_int, C.c_int]
         L.orc_forces_f64.argtypes = [P, _f32p, _f32p, _f64p, C.c_int]
         L.orc_id_hash.argtypes = [C.c_uint32]
         L.orc_id_hash.restype = C.c_uint64
@@ -154,10 +155,10 @@ def ref_cells(p, pos):
     return out.reshape(p.n, 8)
 
 
-def neighbor_sets(p, pos, vel, threads=0):
+def neighbor_sets(p, pos, vel, threads=0, bucketed=True):
     cnt = np.zeros(3 * p.n, np.int32)
     h = np.zeros(3 * p.n, np.uint64)
-    lib().orc_neighbor_sets(C.byref(p), pos, vel, cnt, h, threads)
+    lib().orc_neighbor_sets_ex(C.byref(p), pos, vel, cnt, h, threads, int(bucketed))
     return cnt.reshape(p.n, 3), h.reshape(p.n, 3)
 
 
@@ -211,7 +212,13 @@ class RefEngine:
             cls._libs[kind] = L
         return cls._libs[kind]
 
-    def init(self):
+    def init(self, fresh_drand48=False):
+        """BoidSimulation::init.  fresh_drand48 resets glibc's drand48 state to
+        that of a new process first (the all-pairs engine never seeds it)."""
+        if fresh_drand48:
+            libc = C.CDLL(None)
+            libc.seed48.argtypes = [C.POINTER(C.c_ushort)]
+            libc.seed48((C.c_ushort * 3)(0, 0, 0))
         self.L.ref_init(self.h)
 
     def set_state(self, pos, vel):

@@ -516,11 +516,16 @@ static void nbr_visit(void *vctx, uint32_t i, uint32_t j)
     }
 }
 
-void orc_neighbor_sets(const orc_params *p, const float *pos, const float *vel,
-                       int32_t *count3, uint64_t *hash3, int nthreads)
+void orc_neighbor_sets_ex(const orc_params *p, const float *pos, const float *vel,
+                          int32_t *count3, uint64_t *hash3, int nthreads, int bucketed)
 {
     bucket_t b;
-    bucket_build(&b, p, pos);
+    if (bucketed) {
+        bucket_build(&b, p, pos);
+    } else {
+        b.G = 0;
+        b.start = b.items = NULL;
+    }
     set_threads(nthreads);
 #pragma omp parallel for schedule(dynamic, 64)
     for (int64_t i = 0; i < (int64_t)p->n; i++) {
@@ -531,6 +536,12 @@ void orc_neighbor_sets(const orc_params *p, const float *pos, const float *vel,
         for (int r = 0; r < 3; r++) { count3[3 * i + r] = c.cnt[r]; hash3[3 * i + r] = c.h[r]; }
     }
     bucket_free(&b);
+}
+
+void orc_neighbor_sets(const orc_params *p, const float *pos, const float *vel,
+                       int32_t *count3, uint64_t *hash3, int nthreads)
+{
+    orc_neighbor_sets_ex(p, pos, vel, count3, hash3, nthreads, 1);
 }
 
 /* ------------------------------------------------------------------ FP64 forces */

@@ -70,6 +70,10 @@ int orc_ref_cells(const orc_params *p, const float *pos, int32_t *grid_index8);
 void orc_neighbor_sets(const orc_params *p, const float *pos, const float *vel,
                        int32_t *count3, uint64_t *hash3, int nthreads);
 
+/* As orc_neighbor_sets; bucketed == 0 scans all pairs (the check of the buckets). */
+void orc_neighbor_sets_ex(const orc_params *p, const float *pos, const float *vel,
+                          int32_t *count3, uint64_t *hash3, int nthreads, int bucketed);
+
 /* FP64 restatement of one rule pass: the neighbour sets come from the FP32
  * decisions above and every arithmetic operation is carried out in double.
  * force9 layout matches get_force (coh xyz, sep xyz, ali xyz). */

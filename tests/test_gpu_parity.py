@@ -248,3 +248,46 @@ def test_fp64_oracle_tolerance(boids_lib, oracle_mod):
         s = scale[r]
         assert np.all(err[s == 0] == 0)
         assert np.all(err[s > 0] <= 1e-4 * s[s > 0])
+
+
+# ---------------------------------------------------------------- golden vectors of the reference
+
+import glob as _glob
+import os as _os
+
+from conftest import GOLDEN as _GOLDEN
+
+_GOLDEN_FILES = sorted(_glob.glob(_os.path.join(_GOLDEN, "*.npz")))
+
+
+@pytest.mark.parametrize("path", _GOLDEN_FILES, ids=[_os.path.basename(p)[:-4] for p in _GOLDEN_FILES])
+def test_gpu_reproduces_reference_golden(boids_lib, oracle_mod, path):
+    """The reference engine's own outputs (tests/golden/make_golden.py), from its initial state."""
+    O = oracle_mod
+    g = np.load(path)
+    prm = getattr(O, str(g["settings"]))
+    n, field, steps, engine = int(g["n"]), float(g["field"]), int(g["steps"]), str(g["engine"])
+    sim = make_sim(boids_lib, engine, n, field, prm)
+    sim.set_state(g["pos0"], g["vel0"])
+    sim.update(steps)
+    gp, gv = sim.state()
+    assert_bits_equal(gp, g["pos"], "positions")
+    assert_bits_equal(gv, g["vel"], "velocities")
+    assert_bits_equal(sim.forces(), g["force"], "get_force")
+    if engine == "grid":
+        assert np.array_equal(sim.cells(), g["grid_index"])
+
+
+@pytest.mark.parametrize("path", _GOLDEN_FILES, ids=[_os.path.basename(p)[:-4] for p in _GOLDEN_FILES])
+def test_host_init_reproduces_reference_golden(boids_lib, oracle_mod, path):
+    """BoidSimulation::init's drand48 draws (host side of the library)."""
+    O = oracle_mod
+    g = np.load(path)
+    prm = getattr(O, str(g["settings"]))
+    sim = make_sim(boids_lib, str(g["engine"]), int(g["n"]), float(g["field"]), prm)
+    sim.initialization_type = str(g["init"])
+    sim.rand_seed = int(g["seed"])
+    sim.init()
+    gp, gv = sim.state()
+    assert_bits_equal(gp, g["pos0"], "initial positions")
+    assert_bits_equal(gv, g["vel0"], "initial velocities")
