@@ -78,6 +78,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         if force or not _newer(o, srcs):
             cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "--fmad=false", "-std=c++17",
                    "-Xcompiler", "-fPIC", *inc, "-c", os.path.join(CSRC, src), "-o", o]
+            cmd[1:1] = os.environ.get("BOIDS_NVCC_EXTRA", "").split()  # tuning experiments
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

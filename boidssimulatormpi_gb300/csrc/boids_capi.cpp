@@ -364,7 +364,11 @@ int boids_create(const boids_params *params, boids_sim **out)
         G = g >= 3 ? (int)g : 0;  // fewer than 3 cells per axis: scan all pairs
     }
     k.G = G;
+    k.Gx = 4 * G;
     k.inv_side = G ? (float)(G / p.field_size) : 0.f;
+    k.inv_subx = G ? (float)(4.0 * G / p.field_size) : 0.f;
+    k.side = G ? (float)(p.field_size / G) : 0.f;
+    k.trim_r2 = k.filt_r2 * 1.002f;
     s->engine = G ? 1 : 0;
 
     int rc = 0;
@@ -384,7 +388,7 @@ int boids_create(const boids_params *params, boids_sim **out)
     ALLOC(&b.stage, 6 * n);
     ALLOC(&b.flag, 1, true);
     if (s->engine == 1) {
-        b.ncell = (uint32_t)G * G * G;
+        b.ncell = (uint32_t)(4 * G) * G * G;
         b.ncell_pad = (b.ncell + 1 + boidsgpu::kScanTile - 1) / boidsgpu::kScanTile * boidsgpu::kScanTile;
         b.nscan_blocks = b.ncell_pad / boidsgpu::kScanTile;
         ALLOC(&b.key, n);
@@ -395,10 +399,10 @@ int boids_create(const boids_params *params, boids_sim **out)
         ALLOC(&b.ticket, 1, true);
         const size_t ndense = std::min<size_t>(b.ncell, n / boidsgpu::kDenseMin) + 1;
         ALLOC(&b.dense_list, ndense);
-        ALLOC(&b.dense_n, 1, true);
+        ALLOC(&b.dense_n, 2, true);
         int nsm = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p.device);
-        b.dense_grid = (uint32_t)std::max(1, nsm) * 8;
+        b.dense_grid = (uint32_t)std::max(1, nsm) * 4;
     } else {
         b.ap_cap = boidsgpu::kApCap;
         ALLOC(&b.ap_cnt, n, true);
@@ -740,7 +744,11 @@ int grid_constants_noalloc(const boids_params *params, StepConst *out)
     }
     if (G == 0) return fail(BOIDS_EINVAL, "field too small for device cells: use the handle API");
     k.G = G;
+    k.Gx = 4 * G;
     k.inv_side = (float)(G / p.field_size);
+    k.inv_subx = (float)(4.0 * G / p.field_size);
+    k.side = (float)(p.field_size / G);
+    k.trim_r2 = k.filt_r2 * 1.002f;
     *out = k;
     return BOIDS_OK;
 }

@@ -30,13 +30,17 @@ enum { RULE_COH = 0, RULE_SEP = 1, RULE_ALI = 2 };
 
 struct StepConst {
     uint32_t n;          // boids
-    int32_t G;           // device cells per axis (>= 3), 0 for all-pairs
+    int32_t G;           // device cells per axis along y and z (>= 3), 0 for all-pairs
+    int32_t Gx;          // device cells along x: 4 * G (each a quarter of a y/z cell)
     double F;            // field size (host side only)
     SoftDouble Fsd;      // the field size in integer form, for exact float +- double
     float Ff;            // (float)F, for approximate filters
     float F_dn;          // dn(F): wrap test x > F
     float halfF_dn;      // dn(F/2): minimum-image tests
-    float inv_side;      // cells per unit length of the device grid
+    float inv_side;      // y/z cells per unit length of the device grid
+    float inv_subx;      // x cells per unit length (4 * inv_side)
+    float side;          // y/z cell side (approximate, for row trimming)
+    float trim_r2;       // squared radius, with margin, used to trim a boid's rows
     float filt_r2;       // squared radius of the conservative fast filter
     float box_lim;       // all-pairs box filter: ||dx| - F/2| > box_lim
     float halfFf;        // (float)(F/2) for the box filter
@@ -67,7 +71,7 @@ struct DevBuffers {
     int32_t *dcnt;             // 3 per boid (id order)
     uint64_t *dhash;           // 3 per boid (id order)
     uint32_t *dense_list;      // cells holding >= kDenseMin boids, this step
-    uint32_t *dense_n;         // their number (1 word)
+    uint32_t *dense_n;         // their number, then the dense kernel's work queue (2 words)
     uint32_t *flag;            // set_state range check (1 word)
     uint32_t ncell, ncell_pad, nscan_blocks;
     uint32_t dense_grid;       // CTAs of the dense-cell kernel

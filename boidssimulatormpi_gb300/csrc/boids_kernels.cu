@@ -69,6 +69,24 @@ __device__ __forceinline__ Sight make_sight(float3 v)
     return s;
 }
 
+// The cone tests redone with the exact cosine c = dot / (|v| * |r|)
+// (correctly rounded division and square root, as the reference's floats).
+// Kept out of line: it is rarely needed, and inlined the compiler would
+// predicate it into every candidate test.
+__device__ __noinline__ int cone_flags_exact(float dot, float nv, float d2, float lim0, float lim1, float lim2,
+                                             float cs0, float cs1, float cs2, int round_mask)
+{
+    const float c = __fdiv_rn(dot, __fmul_rn(nv, __fsqrt_rn(d2)));
+    const float lim[3] = {lim0, lim1, lim2}, cs[3] = {cs0, cs1, cs2};
+    int f = 0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const bool in_cone = ((round_mask >> r) & 1) || (c >= cs[r] && c <= 1.0f);  // NaN: false
+        if (d2 < lim[r] && in_cone) f |= 1 << r;
+    }
+    return f;
+}
+
 // The three Boid::isInsideArea tests (src/boid.cpp:27-42) for an imaged
 // target t; bit 0 cohesion, bit 1 separation, bit 2 alignment.
 //
@@ -97,14 +115,9 @@ __device__ __forceinline__ int pair_flags(float3 pi, const Sight &s, float3 t, c
         else if (ca > q.cstar && ca < 1.0f) f |= 1 << r;
     }
     if (exact) {
-        const float c = __fdiv_rn(dot, __fmul_rn(s.nv, __fsqrt_rn(d2)));
-        f = 0;
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            const RuleConst &q = k.rule[r];
-            const bool in_cone = q.all_round || (c >= q.cstar && c <= 1.0f);  // NaN: false
-            if (d2 < q.d2_lim && in_cone) f |= 1 << r;
-        }
+        f = cone_flags_exact(dot, s.nv, d2, k.rule[0].d2_lim, k.rule[1].d2_lim, k.rule[2].d2_lim,
+                             k.rule[0].cstar, k.rule[1].cstar, k.rule[2].cstar,
+                             k.rule[0].all_round | (k.rule[1].all_round << 1) | (k.rule[2].all_round << 2));
     }
     return f;
 }
@@ -235,15 +248,25 @@ __device__ __forceinline__ void integrate(float3 &x, float3 &v, float3 fc, float
 
 // ------------------------------------------------------------------ device grid
 
+// Device cells: side R' (>= the largest radius with margin) along y and z,
+// R'/4 along x.  A y/z "row" of cells is contiguous in the sorted state, and
+// the quarter-width x cells let a boid scan only the x-interval a sphere of
+// radius R' reaches in each neighbouring row.
 __device__ __forceinline__ int cell1(float x, const StepConst &k)
 {
     const int c = __float2int_rz(__fmul_rn(x, k.inv_side));
     return min(max(c, 0), k.G - 1);
 }
 
+__device__ __forceinline__ int subcell_x(float x, const StepConst &k)
+{
+    const int c = __float2int_rz(__fmul_rn(x, k.inv_subx));
+    return min(max(c, 0), k.Gx - 1);
+}
+
 __device__ __forceinline__ uint32_t cell_key(float3 p, const StepConst &k)
 {
-    return (uint32_t)((cell1(p.z, k) * k.G + cell1(p.y, k)) * k.G + cell1(p.x, k));
+    return (uint32_t)((cell1(p.z, k) * k.G + cell1(p.y, k)) * k.Gx + subcell_x(p.x, k));
 }
 
 __device__ __forceinline__ uint32_t cell_start(const uint32_t *__restrict__ lstart,
@@ -382,9 +405,10 @@ k_grid_scan(const uint32_t *__restrict__ count, uint32_t *__restrict__ lstart, u
     const uint32_t v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     uint32_t sum = 0;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        sum += v[i];
-        if (dense_list && v[i] >= (uint32_t)kDenseMin) dense_list[atomicAdd(dense_n, 1u)] = base + i;
+    for (int i = 0; i < 8; ++i) sum += v[i];
+    if (dense_list) {  // a full-size cell is 4 consecutive x cells; base is a multiple of 8
+        if (v[0] + v[1] + v[2] + v[3] >= (uint32_t)kDenseMin) dense_list[atomicAdd(dense_n, 1u)] = base / 4;
+        if (v[4] + v[5] + v[6] + v[7] >= (uint32_t)kDenseMin) dense_list[atomicAdd(dense_n, 1u)] = base / 4 + 1;
     }
     uint32_t total;
     uint32_t run = block_excl_scan<kScanThreads>(sum, warp_tot, total);
@@ -442,38 +466,54 @@ struct Seg {
 
 __device__ __forceinline__ int seg_runs(int cx, const StepConst &k) { return (cx == 0 || cx == k.G - 1) ? 2 : 1; }
 
+// Segment q of the 27 full-size cells around full-size cell (cx, cy, cz),
+// in x-cell indices (4 per full-size cell).
 __device__ __forceinline__ Seg segment(int cx, int cy, int cz, int q, int runs, const StepConst &k)
 {
-    const int G = k.G;
+    const int G = k.G, Gx = k.Gx;
     const int row = q / runs, run = q - row * runs;
     int z = cz + row / 3 - 1, y = cy + row % 3 - 1;
     float sz = 0.f, sy = 0.f;
     if (z < 0) { z += G; sz = -k.Ff; } else if (z >= G) { z -= G; sz = k.Ff; }
     if (y < 0) { y += G; sy = -k.Ff; } else if (y >= G) { y -= G; sy = k.Ff; }
-    const uint32_t r0 = (uint32_t)(z * G + y) * (uint32_t)G;
-    if (runs == 1) return Seg{r0 + cx - 1, r0 + cx + 2, 0.f, sy, sz};
-    if (cx == 0) return run == 0 ? Seg{r0 + G - 1, r0 + G, -k.Ff, sy, sz} : Seg{r0, r0 + 2, 0.f, sy, sz};
-    return run == 0 ? Seg{r0 + G - 2, r0 + G, 0.f, sy, sz} : Seg{r0, r0 + 1, k.Ff, sy, sz};
+    const uint32_t r0 = (uint32_t)(z * G + y) * (uint32_t)Gx;
+    const int x0 = 4 * cx;
+    if (runs == 1) return Seg{r0 + x0 - 4, r0 + x0 + 8, 0.f, sy, sz};
+    if (cx == 0) return run == 0 ? Seg{r0 + Gx - 4, r0 + Gx, -k.Ff, sy, sz} : Seg{r0, r0 + 8, 0.f, sy, sz};
+    return run == 0 ? Seg{r0 + Gx - 8, r0 + Gx, 0.f, sy, sz} : Seg{r0, r0 + 4, k.Ff, sy, sz};
 }
 
 // Which kernel takes the boids of a cell: k_grid_dense when its shared
-// candidate list fits and either the cell is crowded or its neighbourhood is
-// (then sorting once per cell beats sorting per boid), else k_grid_sparse.
+// candidate list fits and either the cell is crowded or it holds a few boids
+// and its neighbourhood is crowded (then sorting once per cell beats sorting
+// per boid), else k_grid_sparse.
+constexpr int kDeferMin = 4;
+
 __device__ __forceinline__ bool dense_path(uint32_t b, uint32_t ncand)
 {
-    return ncand <= (uint32_t)kDenseCap && (b >= (uint32_t)kDenseMin || ncand > (uint32_t)kCandDefer);
+    return ncand <= (uint32_t)kDenseCap &&
+           (b >= (uint32_t)kDenseMin || (b >= (uint32_t)kDeferMin && ncand > (uint32_t)kCandDefer));
 }
 
 // ------------------------------------------------------------------ sparse cells: thread per boid
 
-// All lanes of a warp walk their own candidate lists in lock-step (a flat
-// loop of max-over-warp length).  Candidates passing the squared-distance
-// filter are buffered, and the whole warp runs the exact tests on its
-// buffers together whenever one of them is full, so the expensive test runs
-// with most lanes busy.  Accepted neighbours are kept sorted by id, at most
-// kListCap per pass; a boid with more takes further passes, each keeping the
-// next kListCap ids, so accumulation is always in ascending id.
-constexpr int kBufA = 16;
+// One thread per boid (slot).  In each of the 9 neighbouring y/z rows the
+// boid scans only the x cells a sphere of radius sqrt(trim_r2) around it
+// reaches, and drops rows it cannot reach.
+//
+// All lanes of a warp walk their own candidates in lock-step (a flat loop of
+// max-over-warp length).  Candidates passing the squared-distance filter are
+// buffered, and the whole warp runs the exact tests on its buffers together
+// whenever one of them is full, so the expensive test runs with most lanes
+// busy.  Accepted neighbours are kept sorted by id, at most kListA per pass; a
+// boid with more takes further passes, each keeping the next kListA ids, so
+// accumulation is always in ascending id.  The per-boid tables (segments, hit
+// buffer, sorted list) live in shared memory, one column per thread: as
+// local memory they overflow L1 and every access goes to L2.
+constexpr int kBufA = 12;
+constexpr int kListA = 12;
+constexpr int kRT = 128;      // threads of k_grid_sparse
+constexpr int kSegA = 18;     // at most 9 rows x 2 runs (a run split where x wraps)
 
 struct GridIn {
     const float4 *__restrict__ pos;
@@ -482,31 +522,93 @@ struct GridIn {
     const uint32_t *__restrict__ bsum;
 };
 
+struct SparseSmem {
+    uint32_t seg0[kSegA][kRT];   // first slot | x-shift code << 29 | (row >> 3) << 31
+    uint32_t seg1[kSegA][kRT];   // end slot | (row & 7) << 29
+    uint32_t buf[kBufA][kRT];    // filter hits: slot | shifted << 31
+    uint64_t lst[kListA][kRT];   // accepted neighbours, sorted: id << 32 | slot | flags << 29
+};
+
 template <bool DIAG>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kRT)
 k_grid_sparse(GridIn g, GridOut o, uint32_t *__restrict__ dense_list, uint32_t *__restrict__ dense_n, StepConst k)
 {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ SparseSmem sm;
+    const int G = k.G, Gx = k.Gx;
+    const int t = threadIdx.x;
+    const uint32_t s = blockIdx.x * kRT + t;
     bool act = s < k.n;
     const float4 p4 = act ? g.pos[s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 v4 = act ? g.vel[s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float3 pi = xyz(p4), vi = xyz(v4);
     const int cx = cell1(pi.x, k), cy = cell1(pi.y, k), cz = cell1(pi.z, k);
-    const int runs = seg_runs(cx, k), nseg = 9 * runs;
+    // x-cell index of row (dy, dz) around this boid, with the periodic wrap
+    auto row_base = [&](int r) {
+        int zz = cz + r / 3 - 1, yy = cy + r % 3 - 1;
+        zz = zz < 0 ? zz + G : (zz >= G ? zz - G : zz);
+        yy = yy < 0 ? yy + G : (yy >= G ? yy - G : yy);
+        return (uint32_t)(zz * G + yy) * (uint32_t)Gx;
+    };
+    if (act) {
+        const uint32_t x0 = 4 * (uint32_t)cx, own_row = row_base(4);
+        const uint32_t own0 = cell_start(g.lstart, g.bsum, own_row + x0);
+        const uint32_t b = cell_start(g.lstart, g.bsum, own_row + x0 + 4) - own0;
+        if (b >= (uint32_t)kDeferMin) {
+            // Which kernel: the count of the 27 full-size cells around the
+            // boid's cell, exactly as k_grid_dense computes it.
+            uint32_t ncell27 = 0;
+            const int runs = seg_runs(cx, k);
+            for (int q = 0; q < 9 * runs; ++q) {
+                const Seg sg = segment(cx, cy, cz, q, runs, k);
+                ncell27 += cell_start(g.lstart, g.bsum, sg.c1) - cell_start(g.lstart, g.bsum, sg.c0);
+            }
+            if (dense_path(b, ncell27)) {
+                // a crowded cell is listed by the scan; a cell with a crowded
+                // neighbourhood is listed here, once, by its first boid
+                if (b < (uint32_t)kDenseMin && s == own0)
+                    dense_list[atomicAdd(dense_n, 1u)] = own_row / 4 + (uint32_t)cx;
+                act = false;
+            }
+        }
+    }
+    // This boid's segments: in each neighbour row, the x cells that a sphere
+    // of radius sqrt(trim_r2) around it reaches.
+    int nseg = 0;
     uint32_t ncand = 0;
     if (act) {
-        for (int q = 0; q < nseg; ++q) {
-            const Seg sg = segment(cx, cy, cz, q, runs, k);
-            ncand += cell_start(g.lstart, g.bsum, sg.c1) - cell_start(g.lstart, g.bsum, sg.c0);
-        }
-        const uint32_t cown = (uint32_t)((cz * k.G + cy) * k.G + cx);
-        const uint32_t own0 = cell_start(g.lstart, g.bsum, cown);
-        const uint32_t b = cell_start(g.lstart, g.bsum, cown + 1) - own0;
-        if (dense_path(b, ncand)) {
-            // a crowded cell is listed by the scan; a sparse cell with a
-            // crowded neighbourhood is listed here, once, by its first boid
-            if (b < (uint32_t)kDenseMin && s == own0) dense_list[atomicAdd(dense_n, 1u)] = cown;
-            act = false;
+        const float eps = k.side * 1e-5f;
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+            const int dz = r / 3 - 1, dy = r % 3 - 1;
+            const float ddy = dy == 0 ? 0.f : fmaxf(0.f, dy < 0 ? pi.y - (float)cy * k.side - eps
+                                                              : (float)(cy + 1) * k.side - pi.y - eps);
+            const float ddz = dz == 0 ? 0.f : fmaxf(0.f, dz < 0 ? pi.z - (float)cz * k.side - eps
+                                                              : (float)(cz + 1) * k.side - pi.z - eps);
+            const float rem = k.trim_r2 - ddy * ddy - ddz * ddz;
+            if (!(rem > 0.f)) continue;
+            const float rx = sqrtf(rem);
+            const int lo = __float2int_rd((pi.x - rx) * k.inv_subx);
+            const int hi = __float2int_rd((pi.x + rx) * k.inv_subx);
+            int a0 = lo, a1 = hi + 1, c0 = 0, c1 = 0;  // x-cell runs [a0, a1) and [c0, c1)
+            uint32_t ca = 0, cb = 0;                     // x-shift codes: 1 = -F, 2 = +F
+            if (lo < 0) { a0 = lo + Gx; a1 = Gx; ca = 1; c1 = min(hi + 1, Gx); }
+            else if (hi >= Gx) { a1 = Gx; c1 = hi + 1 - Gx; cb = 2; }
+            const uint32_t rb = row_base(r);
+            const uint32_t rhi = (uint32_t)(r >> 3) << 31, rlo = (uint32_t)(r & 7) << 29;
+            if (a1 > a0) {
+                const uint32_t j0 = cell_start(g.lstart, g.bsum, rb + a0), j1 = cell_start(g.lstart, g.bsum, rb + a1);
+                sm.seg0[nseg][t] = j0 | (ca << 29) | rhi;
+                sm.seg1[nseg][t] = j1 | rlo;
+                ncand += j1 - j0;
+                ++nseg;
+            }
+            if (c1 > c0) {
+                const uint32_t j0 = cell_start(g.lstart, g.bsum, rb + c0), j1 = cell_start(g.lstart, g.bsum, rb + c1);
+                sm.seg0[nseg][t] = j0 | (cb << 29) | rhi;
+                sm.seg1[nseg][t] = j1 | rlo;
+                ncand += j1 - j0;
+                ++nseg;
+            }
         }
     }
     const uint32_t nc = act ? ncand : 0;
@@ -516,64 +618,74 @@ k_grid_sparse(GridIn g, GridOut o, uint32_t *__restrict__ dense_list, uint32_t *
     const Sight sight = make_sight(vi);
     Acc a;
     acc_zero(a);
-    uint64_t lst[kListCap];
-    uint32_t buf[kBufA];
-    int64_t lo = -1;  // ids <= lo were accumulated by earlier passes
+    int64_t lo_id = -1;  // ids <= lo_id were accumulated by earlier passes
     bool need = act;
     while (__any_sync(0xffffffffu, need)) {
         int m = 0, nb = 0;
-        uint32_t more = 0;  // accepted neighbours with id > lo in this pass
-        auto flush = [&]() {
-            for (int q = 0; q < nb; ++q) {
-                const uint32_t j = buf[q];
-                const float4 pj = __ldg(g.pos + j);
-                const uint32_t idj = __float_as_uint(pj.w);
-                if ((int64_t)idj <= lo) continue;
-                const int f = pair_flags(pi, sight, image3(xyz(pj), pi, k), k);
-                if (!f) continue;
-                ++more;
-                const uint64_t e = ((uint64_t)idj << 32) | (uint64_t)(j | ((uint32_t)f << 29));
-                int w;
-                if (m < kListCap) w = m++;
-                else if (e < lst[kListCap - 1]) w = kListCap - 1;
-                else continue;
-                while (w > 0 && lst[w - 1] > e) { lst[w] = lst[w - 1]; --w; }
-                lst[w] = e;
-            }
-            nb = 0;
-        };
+        uint32_t more = 0;  // accepted neighbours with id > lo_id in this pass
         int qs = -1;
-        uint32_t j = 0, jend = 0;
+        uint32_t j = 0, jend = 0;  // global slots [j, jend) of the current segment
+        uint32_t swrap = 0;        // 1 << 31 when the segment crosses a periodic face
         float qx = 0.f, qy = 0.f, qz = 0.f;
         const uint32_t mine = need ? nc : 0;
         for (uint32_t it = 0; it < max_nc; ++it) {
             if (it < mine) {
                 while (j == jend) {  // next non-empty segment
-                    const Seg sg = segment(cx, cy, cz, ++qs, runs, k);
-                    j = cell_start(g.lstart, g.bsum, sg.c0);
-                    jend = cell_start(g.lstart, g.bsum, sg.c1);
-                    qx = pi.x - sg.sx; qy = pi.y - sg.sy; qz = pi.z - sg.sz;
+                    ++qs;
+                    const uint32_t w0 = sm.seg0[qs][t], w1 = sm.seg1[qs][t];
+                    j = w0 & 0x1fffffffu;
+                    jend = w1 & 0x1fffffffu;
+                    const int r = (int)(((w0 >> 31) << 3) | (w1 >> 29));
+                    const uint32_t code = (w0 >> 29) & 3u;
+                    const int dz = r / 3 - 1, dy = r % 3 - 1;
+                    const float sx = code == 1 ? -k.Ff : (code == 2 ? k.Ff : 0.f);
+                    const float sy = cy + dy < 0 ? -k.Ff : (cy + dy >= G ? k.Ff : 0.f);
+                    const float sz = cz + dz < 0 ? -k.Ff : (cz + dz >= G ? k.Ff : 0.f);
+                    qx = pi.x - sx; qy = pi.y - sy; qz = pi.z - sz;
+                    swrap = (code != 0 || sy != 0.f || sz != 0.f) ? 0x80000000u : 0u;
                 }
                 const float4 pj = __ldg(g.pos + j);
                 const float dx = pj.x - qx, dy = pj.y - qy, dz = pj.z - qz;
                 const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                if (d2 < k.filt_r2 && j != s) buf[nb++] = j;
+                if (d2 < k.filt_r2 && j != s) sm.buf[nb++][t] = j | swrap;
                 ++j;
             }
-            if (__any_sync(0xffffffffu, nb == kBufA)) flush();
+            // exact tests of the buffered hits, the whole warp together
+            if (__any_sync(0xffffffffu, nb == kBufA) || it + 1 == max_nc) {
+                for (int q = 0; q < nb; ++q) {
+                    const uint32_t wb = sm.buf[q][t];
+                    const uint32_t jb = wb & 0x7fffffffu;
+                    const float4 pj = __ldg(g.pos + jb);
+                    const uint32_t idj = __float_as_uint(pj.w);
+                    if ((int64_t)idj <= lo_id) continue;
+                    // a filter hit from a segment without periodic shift is nearer
+                    // than F/2 on every axis: it is its own minimum image
+                    const float3 tt = (wb >> 31) ? image3(xyz(pj), pi, k) : xyz(pj);
+                    const int f = pair_flags(pi, sight, tt, k);
+                    if (!f) continue;
+                    ++more;
+                    const uint64_t e = ((uint64_t)idj << 32) | (uint64_t)(jb | ((uint32_t)f << 29));
+                    int w;
+                    if (m < kListA) w = m++;
+                    else if (e < sm.lst[kListA - 1][t]) w = kListA - 1;
+                    else continue;
+                    while (w > 0 && sm.lst[w - 1][t] > e) { sm.lst[w][t] = sm.lst[w - 1][t]; --w; }
+                    sm.lst[w][t] = e;
+                }
+                nb = 0;
+            }
         }
-        flush();
         if (need) {
             for (int q = 0; q < m; ++q) {
-                const uint64_t e = lst[q];
+                const uint64_t e = sm.lst[q][t];
                 const uint32_t jj = (uint32_t)e & 0x1fffffffu;
                 const int f = (int)(((uint32_t)e) >> 29);
-                const float3 t = image3(xyz(__ldg(g.pos + jj)), pi, k);
+                const float3 tt = image3(xyz(__ldg(g.pos + jj)), pi, k);
                 const float3 vj = (f & 4) ? xyz(__ldg(g.vel + jj)) : make_float3(0.f, 0.f, 0.f);
-                acc_add<DIAG>(a, pi, t, vj, f, (uint32_t)(e >> 32));
+                acc_add<DIAG>(a, pi, tt, vj, f, (uint32_t)(e >> 32));
             }
             if (more <= (uint32_t)m) need = false;
-            else lo = (int64_t)(lst[m - 1] >> 32);
+            else lo_id = (int64_t)(sm.lst[m - 1][t] >> 32);
         }
     }
     if (act) finish_boid<DIAG>(a, p4, vi, s, o, k);
@@ -615,39 +727,67 @@ __device__ uint64_t *block_radix_sort(uint64_t *a, uint64_t *b, uint32_t *hist, 
     return a;
 }
 
-constexpr int kDenseThreads = 64;
-constexpr int kBufB = 16;
-constexpr int kDenseK = kDenseCap / kDenseThreads;  // candidates per thread when full
+constexpr int kDT = 128;                       // threads of k_grid_dense
+constexpr int kBufB = 16;                      // filter hits buffered per lane
+constexpr int kChunkList = 32;                 // accepted neighbours a chunk lane hands to its owner
+constexpr int kDenseKT = kDenseCap / kDT;      // candidates per thread when the list is full
 
-// Shared memory of k_grid_dense.  The sort keys and gather slots are dead
-// once the candidates are laid out in id order, so that layout reuses them.
+// Shared memory of k_grid_dense.  Regions whose lifetimes do not overlap
+// share storage: the sort keys become the id-ordered candidate array, and the
+// gather slots and radix histogram become the chunk lists.
 struct DenseSmem {
     union {
         uint64_t keys[2][kDenseCap];  // (id << 16) | (segment << 11) | gather index
-        float4 spos[kDenseCap];       // candidates in id order, moved next to the cell
+        float4 spos[kDenseCap];       // candidates in id order; w = slot | wrapped << 31
     } u;
     union {
-        uint32_t gslot[kDenseCap];    // state slot, by gather index
-        uint32_t sslot[kDenseCap];    // state slot, by id order
+        struct {
+            uint32_t gslot[kDenseCap];      // state slot, by gather index
+            uint32_t hist[16 * kDT];
+        } s;
+        uint32_t lists[kDT * kChunkList];   // (index | flags << 16) per chunk lane
     } v;
-    uint32_t hist[16 * kDenseThreads];
-    uint16_t bufs[kBufB * kDenseThreads];
+    uint16_t bufs[kBufB * kDT];
+    uint16_t nlist[kDT];
+    uint8_t ovf[kDT];
     uint32_t seg_j0[18], seg_k0[19];
     float seg_s[18][3];
-    int nseg;
+    uint32_t work;
 };
-static_assert(sizeof(DenseSmem) <= 48 * 1024, "dense-cell shared memory exceeds the static limit");
 static_assert(kDenseCap <= 2048, "gather index must fit 11 bits");
 
+// The exact image of candidate q of the id-ordered list as seen from pi.
+// Non-wrapped candidates are stored with their exact coordinates and, being
+// nearer than F/2, are their own image; the few across a periodic face are
+// re-read and imaged as the reference does.
+__device__ __forceinline__ float3 cand_image(float4 c, float3 pi, const float4 *__restrict__ pos, const StepConst &k)
+{
+    const uint32_t w = __float_as_uint(c.w);
+    if (w >> 31) return image3(xyz(__ldg(pos + (w & 0x7fffffffu))), pi, k);
+    return xyz(c);
+}
+
+// One CTA takes one crowded cell at a time (dynamic queue).  The cell's
+// 27-cell candidates are radix-sorted by id once.  The cell's b boids x the
+// candidate list is then split over all threads: each boid gets L = 128/b
+// lanes, lane l walks chunk l of the id-ordered list; chunk 0's lane (the
+// owner) accumulates its accepted neighbours at once, the others hand theirs
+// over in id order and the owner folds them in after its own, so the
+// accumulation order stays ascending id.  A chunk lane whose hand-over list
+// overflows leaves its chunk to the owner.
 template <bool DIAG>
-__global__ void __launch_bounds__(kDenseThreads)
-k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, const uint32_t *__restrict__ dense_n,
+__global__ void __launch_bounds__(kDT, 4)
+k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint32_t *__restrict__ dense_n,
              StepConst k)
 {
-    __shared__ DenseSmem sm;
+    extern __shared__ __align__(16) unsigned char dense_smem_raw[];
+    DenseSmem &sm = *reinterpret_cast<DenseSmem *>(dense_smem_raw);
     const int t = threadIdx.x;
-    const uint32_t nd = *dense_n;
-    for (uint32_t w = blockIdx.x; w < nd; w += gridDim.x) {
+    for (;;) {
+        if (t == 0) sm.work = atomicAdd(dense_n + 1, 1u);
+        __syncthreads();
+        const uint32_t w = sm.work;
+        if (w >= dense_n[0]) break;
         const uint32_t c = dense_list[w];
         const int G = k.G;
         const int cx = (int)(c % G), cy = (int)((c / G) % G), cz = (int)(c / ((uint32_t)G * G));
@@ -665,78 +805,135 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, const
         }
         __syncthreads();
         const uint32_t ncand = sm.seg_k0[ns];
-        const uint32_t own0 = cell_start(g.lstart, g.bsum, c);
-        const uint32_t b = cell_start(g.lstart, g.bsum, c + 1) - own0;
+        const uint32_t own0 = cell_start(g.lstart, g.bsum, 4 * c);
+        const uint32_t b = cell_start(g.lstart, g.bsum, 4 * c + 4) - own0;
         if (!dense_path(b, ncand)) {  // too many candidates: left to k_grid_sparse
             __syncthreads();
             continue;
         }
 
-        // gather (id, segment, gather index) keys, sort them by id
-        for (uint32_t q = t; q < ncand; q += kDenseThreads) {
+        // gather (id, segment, gather index) keys and sort them by id
+        for (uint32_t q = t; q < ncand; q += kDT) {
             uint32_t sgi = 0;
             while (q >= sm.seg_k0[sgi + 1]) ++sgi;
             const uint32_t slot = sm.seg_j0[sgi] + (q - sm.seg_k0[sgi]);
-            sm.v.gslot[q] = slot;
+            sm.v.s.gslot[q] = slot;
             sm.u.keys[0][q] = ((uint64_t)__float_as_uint(__ldg(&g.pos[slot].w)) << 16) | (sgi << 11) | q;
         }
         __syncthreads();
-        const uint64_t *sorted = block_radix_sort<kDenseThreads>(sm.u.keys[0], sm.u.keys[1], sm.hist,
-                                                                 (int)ncand, 16, k.id_bits);
-        // lay the candidates out in id order (over the dead sort buffers)
-        const int K = ((int)ncand + kDenseThreads - 1) / kDenseThreads;
+        const uint64_t *sorted =
+            block_radix_sort<kDT>(sm.u.keys[0], sm.u.keys[1], sm.v.s.hist, (int)ncand, 16, k.id_bits);
+        // lay the candidates out in id order over the dead sort buffers
+        const int K = ((int)ncand + kDT - 1) / kDT;
         const int q0 = t * K;
-        uint32_t slot_r[kDenseK], seg_r[kDenseK];
+        uint32_t slot_r[kDenseKT], seg_r[kDenseKT];
 #pragma unroll
-        for (int i = 0; i < kDenseK; ++i) {
+        for (int i = 0; i < kDenseKT; ++i) {
             if (i < K && q0 + i < (int)ncand) {
                 const uint64_t key = sorted[q0 + i];
-                slot_r[i] = sm.v.gslot[(uint32_t)key & 0x7ffu];
+                slot_r[i] = sm.v.s.gslot[(uint32_t)key & 0x7ffu];
                 seg_r[i] = ((uint32_t)key >> 11) & 0x1fu;
             }
         }
         __syncthreads();
 #pragma unroll
-        for (int i = 0; i < kDenseK; ++i) {
+        for (int i = 0; i < kDenseKT; ++i) {
             if (i < K && q0 + i < (int)ncand) {
                 const float4 p = __ldg(g.pos + slot_r[i]);
                 const float *sh = sm.seg_s[seg_r[i]];
-                sm.u.spos[q0 + i] = make_float4(p.x + sh[0], p.y + sh[1], p.z + sh[2], p.w);
-                sm.v.sslot[q0 + i] = slot_r[i];
+                const bool wrapped = sh[0] != 0.f || sh[1] != 0.f || sh[2] != 0.f;
+                sm.u.spos[q0 + i] = wrapped ? make_float4(p.x + sh[0], p.y + sh[1], p.z + sh[2],
+                                                          __uint_as_float(slot_r[i] | 0x80000000u))
+                                            : make_float4(p.x, p.y, p.z, __uint_as_float(slot_r[i]));
             }
         }
         __syncthreads();
 
-        // every boid of the cell walks the candidates in id order; the warp
-        // runs its exact tests together whenever a lane's buffer fills
-        for (uint32_t r0 = 0; r0 < b; r0 += kDenseThreads) {
-            const uint32_t bi = r0 + t;
-            const bool act = bi < b;
-            const uint32_t s = own0 + (act ? bi : 0);
+        for (uint32_t r0 = 0; r0 < b; r0 += kDT) {
+            const uint32_t nbr = min(b - r0, (uint32_t)kDT);      // boids this round
+            const uint32_t L = (uint32_t)kDT / nbr;               // lanes per boid
+            const uint32_t csz = (ncand + L - 1) / L;             // chunk length
+            const bool act = (uint32_t)t < nbr * L;
+            const uint32_t bi = act ? (uint32_t)t % nbr : 0, l = act ? (uint32_t)t / nbr : 0;
+            const uint32_t k0 = act ? min(ncand, l * csz) : 0, k1 = act ? min(ncand, k0 + csz) : 0;
+            const uint32_t s = own0 + r0 + bi;
             const float4 p4 = g.pos[s], v4 = g.vel[s];
             const float3 pi = xyz(p4), vi = xyz(v4);
             const Sight sight = make_sight(vi);
             Acc a;
             acc_zero(a);
-            int nb = 0;
-            auto flush = [&]() {
-                for (int q = 0; q < nb; ++q) {
-                    const uint32_t j = sm.v.sslot[sm.bufs[q * kDenseThreads + t]];
-                    if (j != s) visit<DIAG>(a, pi, sight, g.pos, g.vel, j, k);
+            int nb = 0, nl = 0;
+            bool ovf = false;
+            const uint32_t len = k1 - k0;
+            const uint32_t maxlen = __reduce_max_sync(0xffffffffu, len);
+            for (uint32_t it = 0; it < maxlen; ++it) {
+                if (it < len) {
+                    const uint32_t q = k0 + it;
+                    const float4 cq = sm.u.spos[q];
+                    const float dx = cq.x - pi.x, dy = cq.y - pi.y, dz = cq.z - pi.z;
+                    const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                    if (d2 < k.filt_r2) sm.bufs[nb++ * kDT + t] = (uint16_t)q;
                 }
-                nb = 0;
-            };
-            for (uint32_t q = 0; q < ncand; ++q) {
-                const float4 pj = sm.u.spos[q];
-                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                if (act && d2 < k.filt_r2) sm.bufs[nb++ * kDenseThreads + t] = (uint16_t)q;
-                if (__any_sync(0xffffffffu, nb == kBufB)) flush();
+                // exact tests of the buffered hits, the whole warp together
+                if (__any_sync(0xffffffffu, nb == kBufB) || it + 1 == maxlen) {
+                    for (int e = 0; e < nb; ++e) {
+                        const uint32_t q = sm.bufs[e * kDT + t];
+                        const float4 cq = sm.u.spos[q];
+                        const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
+                        if (j == s) continue;
+                        const float3 tt = cand_image(cq, pi, g.pos, k);
+                        const int f = pair_flags(pi, sight, tt, k);
+                        if (!f) continue;
+                        if (l == 0) {
+                            const float3 vj = (f & 4) ? xyz(__ldg(g.vel + j)) : make_float3(0.f, 0.f, 0.f);
+                            acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
+                        } else if (nl < kChunkList) {
+                            sm.v.lists[t * kChunkList + nl++] = q | ((uint32_t)f << 16);
+                        } else {
+                            ovf = true;
+                        }
+                    }
+                    nb = 0;
+                }
             }
-            flush();
-            if (act) finish_boid<DIAG>(a, p4, vi, s, o, k);
+            sm.nlist[t] = (uint16_t)nl;
+            sm.ovf[t] = ovf;
+            __syncthreads();
+            if (act && l == 0) {
+                // fold the other chunks' neighbours in, in chunk (= id) order
+                for (uint32_t ll = 1; ll < L; ++ll) {
+                    const uint32_t tt_ = ll * nbr + bi;
+                    if (sm.ovf[tt_]) {
+                        const uint32_t c0 = min(ncand, ll * csz), c1 = min(ncand, c0 + csz);
+                        for (uint32_t q = c0; q < c1; ++q) {
+                            const float4 cq = sm.u.spos[q];
+                            const float dx = cq.x - pi.x, dy = cq.y - pi.y, dz = cq.z - pi.z;
+                            const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                            const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
+                            if (!(d2 < k.filt_r2) || j == s) continue;
+                            const float3 tt = cand_image(cq, pi, g.pos, k);
+                            const int f = pair_flags(pi, sight, tt, k);
+                            if (!f) continue;
+                            const float3 vj = (f & 4) ? xyz(__ldg(g.vel + j)) : make_float3(0.f, 0.f, 0.f);
+                            acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
+                        }
+                    } else {
+                        const uint32_t m = sm.nlist[tt_];
+                        for (uint32_t e = 0; e < m; ++e) {
+                            const uint32_t v = sm.v.lists[tt_ * kChunkList + e];
+                            const float4 cq = sm.u.spos[v & 0xffffu];
+                            const int f = (int)(v >> 16);
+                            const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
+                            const float3 tt = cand_image(cq, pi, g.pos, k);
+                            const float3 vj = (f & 4) ? xyz(__ldg(g.vel + j)) : make_float3(0.f, 0.f, 0.f);
+                            acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
+                        }
+                    }
+                }
+                finish_boid<DIAG>(a, p4, vi, s, o, k);
+            }
+            __syncthreads();  // lists and buffers are reused by the next round
         }
-        __syncthreads();  // shared arrays are rebuilt for the next cell
     }
 }
 
@@ -911,7 +1108,7 @@ cudaError_t launch_grid_keys(const StepConst &k, const float4 *pos, uint32_t *ke
 
 cudaError_t launch_grid_scan(const DevBuffers &b, cudaStream_t st, uint64_t *launches)
 {
-    cudaError_t e = cudaMemsetAsync(b.dense_n, 0, sizeof(uint32_t), st);
+    cudaError_t e = cudaMemsetAsync(b.dense_n, 0, 2 * sizeof(uint32_t), st);  // count, work queue
     if (e != cudaSuccess) return e;
     k_grid_scan<<<b.nscan_blocks, kScanThreads, 0, st>>>(b.count, b.lstart, b.bsum, b.ticket, b.nscan_blocks,
                                                           b.dense_list, b.dense_n);
@@ -947,14 +1144,22 @@ cudaError_t launch_grid_force(const StepConst &k, const DevBuffers &b, int from,
         o.count = b.count;
         o.forces = record_forces ? b.forces : nullptr;
     }
-    const unsigned nb = blocks_for(k.n, 128);
+    const unsigned nsp = blocks_for(k.n, kRT);
     const unsigned nd = b.dense_grid;
+    const size_t dsm = sizeof(DenseSmem);
+    static bool attr_set[2] = {false, false};
+    if (!attr_set[diag]) {
+        cudaError_t e = diag ? cudaFuncSetAttribute(k_grid_dense<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm)
+                             : cudaFuncSetAttribute(k_grid_dense<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+        if (e != cudaSuccess) return e;
+        attr_set[diag] = true;
+    }
     if (diag) {
-        k_grid_sparse<true><<<nb, 128, 0, st>>>(g, o, b.dense_list, b.dense_n, k);
-        k_grid_dense<true><<<nd, kDenseThreads, 0, st>>>(g, o, b.dense_list, b.dense_n, k);
+        k_grid_sparse<true><<<nsp, kRT, 0, st>>>(g, o, b.dense_list, b.dense_n, k);
+        k_grid_dense<true><<<nd, kDT, dsm, st>>>(g, o, b.dense_list, b.dense_n, k);
     } else {
-        k_grid_sparse<false><<<nb, 128, 0, st>>>(g, o, b.dense_list, b.dense_n, k);
-        k_grid_dense<false><<<nd, kDenseThreads, 0, st>>>(g, o, b.dense_list, b.dense_n, k);
+        k_grid_sparse<false><<<nsp, kRT, 0, st>>>(g, o, b.dense_list, b.dense_n, k);
+        k_grid_dense<false><<<nd, kDT, dsm, st>>>(g, o, b.dense_list, b.dense_n, k);
     }
     *launches += 2;
     return cudaGetLastError();

@@ -67,7 +67,7 @@ size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
 size_t layout(const boidsgpu::StepConst &k, unsigned char *base, boidsgpu::DevBuffers *b)
 {
     const size_t n = k.n ? k.n : 1;
-    b->ncell = (uint32_t)k.G * k.G * k.G;
+    b->ncell = (uint32_t)k.Gx * k.G * k.G;
     b->ncell_pad = (b->ncell + 1 + boidsgpu::kScanTile - 1) / boidsgpu::kScanTile * boidsgpu::kScanTile;
     b->nscan_blocks = b->ncell_pad / boidsgpu::kScanTile;
     const size_t ndense = (b->ncell < n / boidsgpu::kDenseMin ? b->ncell : n / boidsgpu::kDenseMin) + 1;
@@ -88,7 +88,7 @@ size_t layout(const boidsgpu::StepConst &k, unsigned char *base, boidsgpu::DevBu
     b->bsum = reinterpret_cast<uint32_t *>(take(4 * (size_t)b->nscan_blocks));
     b->ticket = reinterpret_cast<uint32_t *>(take(4));
     b->dense_list = reinterpret_cast<uint32_t *>(take(4 * ndense));
-    b->dense_n = reinterpret_cast<uint32_t *>(take(4));
+    b->dense_n = reinterpret_cast<uint32_t *>(take(8));
     return off;
 }
 
@@ -123,7 +123,7 @@ extern "C" int boids_step_noalloc(const boids_params *params, const float *pos3n
     layout(k, base, &b);
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, params->device);
-    b.dense_grid = (uint32_t)(nsm > 0 ? nsm : 1) * 8;
+    b.dense_grid = (uint32_t)(nsm > 0 ? nsm : 1) * 4;
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     uint64_t launches = 0;
     // the array keeps the previous call's contents: clear what must start at zero
