@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--boids", dest="n", type=int, default=1 << 20)
     ap.add_argument("--field", type=float, default=4.0)
     ap.add_argument("--seed", type=int, default=12345)
     ap.add_argument("--engine", choices=["grid", "allpairs"], default="grid")
@@ -79,6 +79,19 @@ def dist_setup(a):
         dist.init_process_group(backend)
         return dist.get_rank(), ws, dist
     return 0, 1, None
+
+
+def reduce_over_ranks(dist, seconds, units, device=None):
+    """Replicas: the slowest rank's time and the boid-steps of all ranks
+    (value = units / seconds).  No collective on one rank."""
+    if dist is None:
+        return seconds, units
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    u = torch.tensor([units], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
 
 
 # ------------------------------------------------------------------ clocks
@@ -262,12 +275,9 @@ def run_ours(a):
     prof = sim.profile_read(True)
     sim.profile_enable(False)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    if dist is not None:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = a.n * a.steps * ws / (total_ms / 1e3)
+    total_s, units = reduce_over_ranks(dist, sum(step_ms) / 1e3, float(a.n * a.steps), dev)
+    total_ms = total_s * 1e3
+    value = units / total_s
 
     # ---- end to end through the C ABI with host buffers
     hp = torch.empty(3 * a.n, dtype=torch.float32, pin_memory=True).numpy()
@@ -281,12 +291,8 @@ def run_ours(a):
         sim.update(1)
         sim.state(hp, hv)
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": a.n * a.steps * ws / e2e_s, "unit": UNIT,
+    e2e_s, e2e_units = reduce_over_ranks(dist, time.perf_counter() - t0, float(a.n * a.steps), dev)
+    e2e = {"value": e2e_units / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(hp.nbytes + hv.nbytes),
            "d2h_bytes_per_step": int(hp.nbytes + hv.nbytes)}
 

@@ -75,6 +75,21 @@ SIGNATURES = {
     "boids_profile_enable": (C.c_int, [_vp, C.c_int32]),
     "boids_profile_read": (C.c_int, [_vp, C.POINTER(Profile), C.c_int32]),
     "boids_kernel_launches": (C.c_uint64, [_vp]),
+    "boids_frame_async": (C.c_int, [_vp, _vp, _vp, C.c_int32, C.c_int32]),
+    "boids_frame_wait": (C.c_int, [_vp, C.c_int32]),
+    "boids_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_vp)]),
+    "boids_host_free": (None, [_vp]),
+    "boids_ensemble_create": (C.c_int, [_vp, C.c_uint32, C.POINTER(_vp)]),
+    "boids_ensemble_destroy": (None, [_vp]),
+    "boids_ensemble_init": (C.c_int, [_vp]),
+    "boids_ensemble_set_state": (C.c_int, [_vp, C.c_uint32, _vp, _vp]),
+    "boids_ensemble_step": (C.c_int, [_vp, C.c_int32]),
+    "boids_ensemble_get_state": (C.c_int, [_vp, C.c_uint32, _vp, _vp]),
+    "boids_ensemble_stats": (C.c_int, [_vp, _vp]),
+    "boids_ensemble_autotune": (C.c_int, [_vp, C.c_int32]),
+    "boids_ensemble_tuning": (C.c_int, [_vp, _vp]),
+    "boids_ensemble_synchronize": (C.c_int, [_vp]),
+    "boids_ensemble_kernel_launches": (C.c_uint64, [_vp]),
     "boids_step_noalloc": (C.c_int, [C.POINTER(Params), _vp, _vp, _vp, _vp, _vp]),
     "boids_last_error": (C.c_char_p, []),
     "boids_version": (C.c_char_p, []),
@@ -263,3 +278,86 @@ class BoidSimulation:
 
 def version() -> str:
     return lib().boids_version().decode()
+
+
+# ------------------------------------------------------------------ ensembles
+
+INIT_RANDOM_UNIFORM = 0
+INIT_TEST = 1
+STAT_NAMES = ("polarization", "milling", "nn_distance", "largest_cluster", "com_x", "com_y", "com_z",
+              "momentum_x", "momentum_y", "momentum_z", "search_radius")
+
+
+class FlockDesc(C.Structure):
+    _fields_ = [("params", Params), ("init_kind", C.c_int32), ("rand_seed", C.c_int32)]
+
+
+def flock_params(n, field, sep, ali, coh, vmax, vmin, device=0):
+    """Params of one grid-engine flock; sep/ali/coh are (distance, angle, coefficient)."""
+    return Params(n, field, *sep, *ali, *coh, vmax, vmin, ENGINE_GRID, device, 0, 0)
+
+
+class Ensemble:
+    """Many independent grid-engine flocks stepped together (boids_ensemble_*).
+
+    ``flocks`` is a list of (Params, init_kind, rand_seed).  Each flock's
+    trajectory is bit-identical to a BoidSimulation("grid") with the same
+    parameters and seed."""
+
+    def __init__(self, flocks):
+        arr = (FlockDesc * len(flocks))()
+        for i, (p, kind, seed) in enumerate(flocks):
+            arr[i] = FlockDesc(p, kind, seed)
+        h = C.c_void_p()
+        _check(lib().boids_ensemble_create(C.cast(arr, C.c_void_p), len(flocks), C.byref(h)))
+        self.h = h
+        self.sizes = [p.number_of_agents for p, _, _ in flocks]
+
+    def init(self):
+        _check(lib().boids_ensemble_init(self.h))
+
+    def step(self, steps=1):
+        _check(lib().boids_ensemble_step(self.h, steps))
+
+    def synchronize(self):
+        _check(lib().boids_ensemble_synchronize(self.h))
+
+    def set_state(self, flock, pos, vel):
+        n = self.sizes[flock]
+        p, v = _f32(pos, 3 * n), _f32(vel, 3 * n)
+        _check(lib().boids_ensemble_set_state(self.h, flock, _ptr(p), _ptr(v)))
+
+    def state(self, flock):
+        n = self.sizes[flock]
+        p = np.empty(3 * n, np.float32)
+        v = np.empty(3 * n, np.float32)
+        _check(lib().boids_ensemble_get_state(self.h, flock, _ptr(p), _ptr(v)))
+        return p.reshape(n, 3), v.reshape(n, 3)
+
+    def stats(self):
+        out = np.empty((len(self.sizes), len(STAT_NAMES)), np.float64)
+        _check(lib().boids_ensemble_stats(self.h, _ptr(out)))
+        return out
+
+    def autotune(self, steps_per_trial=0):
+        _check(lib().boids_ensemble_autotune(self.h, steps_per_trial))
+        return self.tuning()
+
+    def tuning(self):
+        t = np.zeros(3, np.int32)
+        _check(lib().boids_ensemble_tuning(self.h, _ptr(t)))
+        return tuple(int(x) for x in t)
+
+    def kernel_launches(self):
+        return int(lib().boids_ensemble_kernel_launches(self.h))
+
+    def close(self):
+        if self.h is not None and _lib is not None:
+            _lib.boids_ensemble_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

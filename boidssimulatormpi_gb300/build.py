@@ -82,7 +82,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)
-    cpp = ["boids_capi.cpp"]
+    cpp = ["boids_capi.cpp", "boids_ensemble.cpp"]
     for src in cpp:
         o = obj(os.path.splitext(src)[0])
         if force or not _newer(o, _sources(src) + HEADERS):
@@ -93,7 +93,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for r in ex.map(_run, jobs):
             out.append(r)
-    objs = [obj("boids_kernels"), obj("boids_noalloc"), obj("boids_capi")]
+    objs = [obj("boids_kernels"), obj("boids_noalloc"), obj("boids_capi"), obj("boids_ensemble")]
     if force or jobs or not os.path.exists(LIB):
         tmp = LIB + ".tmp%d" % os.getpid()
         _run(["g++", "-shared", "-o", tmp, *objs, "-L" + os.path.join(cuda, "lib64"),
@@ -107,7 +107,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
             exe = os.path.join(BIN, name)
             if force or not _newer(exe, cli_src + HEADERS + [LIB]):
                 _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-Wall", *inc,
-                      "-DBOIDSIM_ENGINE=" + engine, cli_src[0], cli_src[1], "-o", exe,
+                      "-DBOIDSIM_ENGINE=" + engine, cli_src[0], cli_src[1], "-o", exe, "-pthread",
                       "-L" + PKG, "-lboids_gb300", "-Wl,-rpath,$ORIGIN/.."])
     if verbose:
         sys.stdout.write("".join(out))

@@ -153,6 +153,10 @@ struct boids_sim {
     std::vector<Pending> pending;
     std::vector<cudaEvent_t> pool;
     boids_profile_t acc{};
+    // .ptcl frames: device assembly buffer (15 floats per boid) and one
+    // completion event per slot, made on first use
+    float *frame_dev = nullptr;
+    cudaEvent_t frame_ev[BOIDS_FRAME_SLOTS] = {};
 };
 
 namespace {
@@ -265,19 +269,45 @@ int grid_bin_fresh(boids_sim *s)
     return 0;
 }
 
-}  // namespace
-
-extern "C" {
-
-const char *boids_last_error(void) { return g_err.c_str(); }
-
-const char *boids_version(void) { return "boids_gb300 0.1 (sm_103a)"; }
-
-int boids_create(const boids_params *params, boids_sim **out)
+// The drawn placements of BoidSimulation::init, in the reference's draw
+// order (src/boid_simulation_grid.cpp:95-136; the all-pairs engine's
+// src/boid_simulation.cpp:79-112 draws the same sequence but never calls
+// srand48: seeded == false starts from the never-seeded state).
+void draw_state(const boids_params &p, bool test, bool seeded, int32_t seed, float *pos, float *vel)
 {
-    if (!params || !out) return fail(BOIDS_EINVAL, "boids_create: null argument");
-    *out = nullptr;
-    const boids_params &p = *params;
+    const double F = p.field_size;
+    Drand48 d;
+    if (seeded) d.seed((long)seed);
+    const double vmax = p.velocity_max, vmin = p.velocity_min;
+    for (uint32_t i = 0; i < p.number_of_agents; ++i) {
+        float *x = pos + (size_t)3 * i, *v = vel + (size_t)3 * i;
+        if (test) {  // src/boid_simulation_grid.cpp:100-108
+            x[0] = (float)(F * 3 / 8 + d.next() * F / 4);
+            x[1] = (float)(F * 3 / 8 + d.next() * F / 4);
+            if (d.next() > 0.5) x[2] = (float)(d.next() * F / 4 + F * 3 / 4);
+            else x[2] = (float)(d.next() * F / 4);
+        } else {  // src/boid_simulation_grid.cpp:123-126
+            x[0] = (float)(F * d.next());
+            x[1] = (float)(F * d.next());
+            x[2] = (float)(F * d.next());
+        }
+        // src/boid_simulation_grid.cpp:127-132
+        const double sp = d.next() * (vmax - vmin) + vmin;
+        const double th1 = d.next() * M_PI;
+        const double th2 = d.next() * 2.0 * M_PI;
+        v[0] = (float)(sp * std::sin(th1) * std::cos(th2));
+        v[1] = (float)(sp * std::sin(th1) * std::sin(th2));
+        v[2] = (float)(sp * std::cos(th1));
+    }
+}
+
+// The parameter-derived constants of one flock: the exact float thresholds,
+// the reference's overlapping-grid geometry (src/boid_simulation_grid.cpp:80-89,
+// whose checks apply to the grid engine) and this engine's device grid (G = 0:
+// too few cells per axis, scan all pairs).  *ref_ok: the reference geometry
+// is valid (boids_get_cells).
+int make_constants(const boids_params &p, StepConst &k, bool *ref_ok)
+{
     if (p.number_of_agents > boidsgpu::kMaxBoids)
         return fail(BOIDS_EINVAL, "number_of_agents exceeds 2^29");
     if (!(p.field_size > 0.0) || !std::isfinite(p.field_size))
@@ -288,9 +318,7 @@ int boids_create(const boids_params *params, boids_sim **out)
     for (double r : radii)
         if (std::isnan(r)) return fail(BOIDS_EINVAL, "sight distance is NaN");
 
-    boids_sim *s = new boids_sim();
-    s->p = p;
-    StepConst &k = s->k;
+    k = StepConst{};
     k.n = p.number_of_agents;
     k.F = p.field_size;
     k.Ff = (float)p.field_size;
@@ -320,8 +348,7 @@ int boids_create(const boids_params *params, boids_sim **out)
         q.all_round = ang[r] >= 1.0;
         q.cstar = INFINITY;
         if (!q.all_round) {
-            int rc = cone_threshold(ang[r], &q.cstar);
-            if (rc) { delete s; return rc; }
+            if (int rc = cone_threshold(ang[r], &q.cstar)) return rc;
         }
         k.d2_any = std::fmax(k.d2_any, q.d2_lim);
         const float rup = f_up(radii[r]);
@@ -338,18 +365,14 @@ int boids_create(const boids_params *params, boids_sim **out)
     // reference overlapping-grid geometry
     float refR = 0.f, refGS = 0.f;
     int refG = 0;
-    s->ref_geometry_ok = ref_geometry(p, &refR, &refG, &refGS);
+    *ref_ok = ref_geometry(p, &refR, &refG, &refGS);
     if (p.engine == BOIDS_ENGINE_GRID) {
-        if (!s->ref_geometry_ok) {
-            delete s;
+        if (!*ref_ok)
             return fail(BOIDS_EINVAL, "Invalid GRID_NUM: the reference grid engine needs "
                                       "field_size > 2 * max sight distance (src/boid_simulation_grid.cpp:86-89)");
-        }
-        if (refG == 1) {
-            delete s;
+        if (refG == 1)
             return fail(BOIDS_EINVAL, "GRID_NUM == 1: the reference grid engine lists a boid up to 8 times in "
                                       "its own cell (overlap cell == own cell); use the all-pairs engine");
-        }
     }
     k.refG = refG;
     k.refGS = refGS;
@@ -369,7 +392,35 @@ int boids_create(const boids_params *params, boids_sim **out)
     k.inv_subx = G ? (float)(4.0 * G / p.field_size) : 0.f;
     k.side = G ? (float)(p.field_size / G) : 0.f;
     k.trim_r2 = k.filt_r2 * 1.002f;
-    s->engine = G ? 1 : 0;
+    k.dense_min = boidsgpu::kDenseMin;
+    k.defer_min = boidsgpu::kDeferMin;
+    k.cand_defer = boidsgpu::kCandDefer;
+    return BOIDS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *boids_last_error(void) { return g_err.c_str(); }
+
+const char *boids_version(void) { return "boids_gb300 0.1 (sm_103a)"; }
+
+int boids_create(const boids_params *params, boids_sim **out)
+{
+    if (!params || !out) return fail(BOIDS_EINVAL, "boids_create: null argument");
+    *out = nullptr;
+    const boids_params &p = *params;
+    StepConst kc{};
+    bool ref_ok = false;
+    if (int rc = make_constants(p, kc, &ref_ok)) return rc;
+    boids_sim *s = new boids_sim();
+    s->p = p;
+    s->k = kc;
+    s->ref_geometry_ok = ref_ok;
+    s->engine = kc.G ? 1 : 0;
+    const StepConst &k = s->k;
+    const int G = k.G;
 
     int rc = 0;
     if ((rc = use_device(s))) { delete s; return rc; }
@@ -397,12 +448,13 @@ int boids_create(const boids_params *params, boids_sim **out)
         ALLOC(&b.lstart, b.ncell_pad);
         ALLOC(&b.bsum, b.nscan_blocks);
         ALLOC(&b.ticket, 1, true);
-        const size_t ndense = std::min<size_t>(b.ncell, n / boidsgpu::kDenseMin) + 1;
+        const size_t ndense = boidsgpu::dense_list_capacity(b.ncell, n);
         ALLOC(&b.dense_list, ndense);
         ALLOC(&b.dense_n, 2, true);
         int nsm = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p.device);
         b.dense_grid = (uint32_t)std::max(1, nsm) * 4;
+        b.dense_min = k.dense_min;
     } else {
         b.ap_cap = boidsgpu::kApCap;
         ALLOC(&b.ap_cnt, n, true);
@@ -427,6 +479,9 @@ void boids_destroy(boids_sim *s)
     cudaSetDevice(s->p.device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_buffers(s->b);
+    if (s->frame_dev) cudaFree(s->frame_dev);
+    for (cudaEvent_t e : s->frame_ev)
+        if (e) cudaEventDestroy(e);
     resolve_events(s);
     for (cudaEvent_t e : s->pool) cudaEventDestroy(e);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -468,34 +523,11 @@ int boids_init_ex(boids_sim *s, const char *init, int32_t seed, int32_t seed_mod
 {
     if (!s || !init) return fail(BOIDS_EINVAL, "boids_init: null argument");
     const uint32_t n = s->k.n;
-    const double F = s->p.field_size;
     std::vector<float> pos((size_t)3 * n), vel((size_t)3 * n);
     const std::string kind(init);
     if (kind == "test" || kind == "random_uniform") {
         const bool seeded = seed_mode < 0 ? s->p.engine == BOIDS_ENGINE_GRID : seed_mode != 0;
-        Drand48 d;
-        if (seeded) d.seed((long)seed);
-        const double vmax = s->p.velocity_max, vmin = s->p.velocity_min;
-        for (uint32_t i = 0; i < n; ++i) {
-            float *x = &pos[(size_t)3 * i], *v = &vel[(size_t)3 * i];
-            if (kind == "test") {  // src/boid_simulation_grid.cpp:100-108
-                x[0] = (float)(F * 3 / 8 + d.next() * F / 4);
-                x[1] = (float)(F * 3 / 8 + d.next() * F / 4);
-                if (d.next() > 0.5) x[2] = (float)(d.next() * F / 4 + F * 3 / 4);
-                else x[2] = (float)(d.next() * F / 4);
-            } else {  // src/boid_simulation_grid.cpp:123-126
-                x[0] = (float)(F * d.next());
-                x[1] = (float)(F * d.next());
-                x[2] = (float)(F * d.next());
-            }
-            // src/boid_simulation_grid.cpp:127-132
-            const double sp = d.next() * (vmax - vmin) + vmin;
-            const double th1 = d.next() * M_PI;
-            const double th2 = d.next() * 2.0 * M_PI;
-            v[0] = (float)(sp * std::sin(th1) * std::cos(th2));
-            v[1] = (float)(sp * std::sin(th1) * std::sin(th2));
-            v[2] = (float)(sp * std::cos(th1));
-        }
+        draw_state(s->p, kind == "test", seeded, seed, pos.data(), vel.data());
     } else {
         // raw float32 x,y,z,vx,vy,vz per boid (src/boid_simulation.cpp:113-136)
         std::ifstream f(kind, std::ios::binary);
@@ -576,6 +608,58 @@ int boids_get_forces(boids_sim *s, float *force9n)
     if (rc) return rc;
     CK(cudaMemcpyAsync(force9n, s->b.forces, sizeof(float) * 9 * s->k.n, cudaMemcpyDeviceToHost, s->stream));
     return boids_synchronize(s);
+}
+
+int boids_frame_async(boids_sim *s, float *pframe, float *vframe, int32_t with_forces, int32_t slot)
+{
+    if (!s || !pframe || slot < 0 || slot >= BOIDS_FRAME_SLOTS)
+        return fail(BOIDS_EINVAL, "boids_frame_async: bad argument");
+    if (!s->has_state) return fail(BOIDS_ESTATE, "boids_frame_async: no state");
+    if (with_forces && !s->b.forces)
+        return fail(BOIDS_ESTATE, "boids_frame_async: forces need a handle made with BOIDS_FLAG_RECORD_FORCES");
+    int rc = use_device(s);
+    if (rc) return rc;
+    const size_t n = s->k.n;
+    if (!s->frame_dev && (rc = dalloc(&s->frame_dev, 15 * n))) return rc;
+    if (!s->frame_ev[slot]) CK(cudaEventCreateWithFlags(&s->frame_ev[slot], cudaEventDisableTiming));
+    const size_t stride = with_forces ? 12 : 3;
+    float *dp = s->frame_dev, *dv = s->frame_dev + 12 * n;
+    {
+        PhaseTimer t(s, 2);
+        CK(boidsgpu::launch_frame(s->b.pos[s->cur], s->b.vel[s->cur], s->forces_valid ? s->b.forces : nullptr,
+                                  dp, vframe ? dv : nullptr, with_forces ? 1 : 0, (uint32_t)n, s->stream,
+                                  &s->launches));
+        CK(cudaMemcpyAsync(pframe, dp, sizeof(float) * stride * n, cudaMemcpyDeviceToHost, s->stream));
+        if (vframe) CK(cudaMemcpyAsync(vframe, dv, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s->stream));
+    }
+    CK(cudaEventRecord(s->frame_ev[slot], s->stream));
+    return BOIDS_OK;
+}
+
+int boids_frame_wait(boids_sim *s, int32_t slot)
+{
+    if (!s || slot < 0 || slot >= BOIDS_FRAME_SLOTS) return fail(BOIDS_EINVAL, "boids_frame_wait: bad argument");
+    if (!s->frame_ev[slot]) return BOIDS_OK;  // nothing was queued on this slot
+    CK(cudaEventSynchronize(s->frame_ev[slot]));
+    return BOIDS_OK;
+}
+
+int boids_host_alloc(size_t bytes, void **out)
+{
+    if (!out) return fail(BOIDS_EINVAL, "boids_host_alloc: null argument");
+    *out = nullptr;
+    cudaError_t e = cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        cudaGetLastError();
+        return fail(BOIDS_ENOMEM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+    }
+    return BOIDS_OK;
+}
+
+void boids_host_free(void *p)
+{
+    if (p) cudaFreeHost(p);
 }
 
 int boids_get_cells(boids_sim *s, int32_t *gi8)
@@ -676,79 +760,32 @@ int set_last_error(int code, const char *msg) { return fail(code, msg); }
 // The step constants boids_create derives for a grid-engine handle, for the
 // allocation-free entry point, which has no handle.  Uses no heap memory on
 // success.
+int flock_constants(const boids_params *params, StepConst *out, const char *who)
+{
+    const boids_params &p = *params;
+    if (p.engine != BOIDS_ENGINE_GRID) return fail(BOIDS_EINVAL, std::string(who) + ": grid engine only");
+    StepConst k{};
+    bool ref_ok = false;
+    if (int rc = make_constants(p, k, &ref_ok)) return rc;
+    if (k.G == 0) return fail(BOIDS_EINVAL, std::string(who) + ": field too small for device cells (fewer than 3 "
+                                                          "per axis); use a boids_create handle");
+    *out = k;
+    return BOIDS_OK;
+}
+
+void draw_initial_state(const boids_params *p, int test, int32_t seed, float *pos, float *vel)
+{
+    draw_state(*p, test != 0, true, seed, pos, vel);
+}
+
 int grid_constants_noalloc(const boids_params *params, StepConst *out)
 {
     const boids_params &p = *params;
-    if (p.number_of_agents > kMaxBoids) return fail(BOIDS_EINVAL, "number_of_agents exceeds 2^29");
-    if (!(p.field_size > 0.0) || !std::isfinite(p.field_size))
-        return fail(BOIDS_EINVAL, "field_size must be positive and finite");
     if (p.engine != BOIDS_ENGINE_GRID) return fail(BOIDS_EINVAL, "boids_step_noalloc runs the grid engine only");
-    const double radii[3] = {p.cohesion_sight_distance, p.separation_sight_distance, p.alignment_sight_distance};
-    for (double r : radii)
-        if (std::isnan(r)) return fail(BOIDS_EINVAL, "sight distance is NaN");
     StepConst k{};
-    k.n = p.number_of_agents;
-    k.F = p.field_size;
-    k.Ff = (float)p.field_size;
-    k.F_dn = f_dn(p.field_size);
-    k.halfF_dn = f_dn(p.field_size / 2);
-    k.halfFf = (float)(p.field_size / 2);
-    k.cc = (float)p.cohesion_force_coefficient;
-    k.cs = (float)p.separation_force_coefficient;
-    k.ca = (float)p.alignment_force_coefficient;
-    k.vmax_dn = f_dn(p.velocity_max);
-    k.vmin_up = f_up(p.velocity_min);
-    k.vmax_f = (float)p.velocity_max;
-    k.vmin_f = (float)p.velocity_min;
-    k.Fsd = soft_double(p.field_size);
-    k.cone_band = 4e-6f;
-    int bits = 0;
-    while (bits < 32 && (1ull << bits) < (uint64_t)(k.n ? k.n : 1)) ++bits;
-    k.id_bits = std::max(4, (bits + 3) / 4 * 4);
-    const double ang[3] = {p.cohesion_sight_angle, p.separation_sight_angle, p.alignment_sight_angle};
-    float rmax = 0.f;
-    for (int r = 0; r < 3; ++r) {
-        RuleConst &q = k.rule[r];
-        q.d2_lim = radius_d2_limit(radii[r]);
-        q.all_round = ang[r] >= 1.0;
-        q.cstar = INFINITY;
-        if (!q.all_round) {
-            const int rc = cone_threshold(ang[r], &q.cstar);
-            if (rc) return rc;
-        }
-        k.d2_any = std::fmax(k.d2_any, q.d2_lim);
-        const float rup = f_up(radii[r]);
-        if (rup > rmax) rmax = rup;
-    }
-    const double ulpF = std::nextafter(std::fmax(k.Ff, 1.0f), INFINITY) - std::fmax(k.Ff, 1.0f);
-    const double rf = (double)rmax * (1.0 + 1e-4) + 8.0 * ulpF;
-    k.filt_r2 = (float)(rf * rf);
-    k.box_lim = (float)(p.field_size / 2 - rf * (1.0 + 1e-4) - 8.0 * ulpF);
-    float refR = 0.f, refGS = 0.f;
-    int refG = 0;
-    if (!ref_geometry(p, &refR, &refG, &refGS))
-        return fail(BOIDS_EINVAL, "Invalid GRID_NUM: the reference grid engine needs "
-                                  "field_size > 2 * max sight distance (src/boid_simulation_grid.cpp:86-89)");
-    if (refG == 1)
-        return fail(BOIDS_EINVAL, "GRID_NUM == 1: the reference grid engine lists a boid up to 8 times in "
-                                  "its own cell; use the all-pairs engine");
-    k.refG = refG;
-    k.refGS = refGS;
-    k.refR = refR;
-    int G = 0;
-    if (rf > 0) {
-        double g = std::floor(p.field_size / (rf * 1.01));
-        const double cap = std::cbrt(std::fmax(2.0 * k.n, 2097152.0));
-        if (g > cap) g = std::floor(cap);
-        G = g >= 3 ? (int)g : 0;
-    }
-    if (G == 0) return fail(BOIDS_EINVAL, "field too small for device cells: use the handle API");
-    k.G = G;
-    k.Gx = 4 * G;
-    k.inv_side = (float)(G / p.field_size);
-    k.inv_subx = (float)(4.0 * G / p.field_size);
-    k.side = (float)(p.field_size / G);
-    k.trim_r2 = k.filt_r2 * 1.002f;
+    bool ref_ok = false;
+    if (int rc = make_constants(p, k, &ref_ok)) return rc;
+    if (k.G == 0) return fail(BOIDS_EINVAL, "field too small for device cells: use the handle API");
     *out = k;
     return BOIDS_OK;
 }

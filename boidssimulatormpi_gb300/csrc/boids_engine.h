@@ -54,6 +54,33 @@ struct StepConst {
     // the reference's overlapping grid, for Boid::grid_index parity
     int32_t refG;
     float refGS, refR;
+    // Place of this flock in a batched ensemble (all zero for one flock):
+    // its cells are global cells [cell_base, cell_base + Gx*G*G), its boids
+    // occupy state slots [slot_base, slot_base + n), and slot = cell start
+    // (a prefix over all flocks' counts) + slot_off, the padding that aligns
+    // every flock to kSlotAlign slots.  Boid ids are local to the flock.
+    uint32_t cell_base;
+    uint32_t slot_base;
+    uint32_t slot_off;
+    uint32_t flock;
+    // Which full-size cells the CTA-per-cell kernel takes (the results do not
+    // depend on it): those holding dense_min boids or more, and those holding
+    // defer_min or more whose 27-cell neighbourhood holds over cand_defer
+    // boids.  kDeferMin <= defer_min <= dense_min.
+    uint32_t dense_min, defer_min, cand_defer;
+    uint32_t pad2;
+};
+
+// A batched ensemble's flock table, in device memory.  Every block of
+// kSlotAlign state slots belongs to one flock, so a CTA of that many threads
+// serves one flock and can hold its StepConst in shared memory.
+constexpr int kSlotAlign = 128;
+struct FlockTable {
+    const StepConst *ks;        // per flock
+    const uint16_t *blk_flock;  // per block of kSlotAlign slots
+    const uint32_t *cell4;      // per flock: cell_base / 4 (ascending)
+    uint32_t count;             // flocks
+    uint32_t nslots;            // padded slots of all flocks
 };
 
 // Device scratch of one engine handle.  Sizes in elements.
@@ -70,19 +97,31 @@ struct DevBuffers {
     int32_t *cells8;           // 8 per boid (id order)
     int32_t *dcnt;             // 3 per boid (id order)
     uint64_t *dhash;           // 3 per boid (id order)
-    uint32_t *dense_list;      // cells holding >= kDenseMin boids, this step
+    uint32_t *dense_list;      // full-size cells for the dense kernel, this step (dense_list_capacity)
     uint32_t *dense_n;         // their number, then the dense kernel's work queue (2 words)
     uint32_t *flag;            // set_state range check (1 word)
     uint32_t ncell, ncell_pad, nscan_blocks;
     uint32_t dense_grid;       // CTAs of the dense-cell kernel
+    uint32_t dense_min;        // the scan's listing threshold (= StepConst::dense_min)
     uint32_t ap_cap;
 };
 
 constexpr int kScanTile = 2048;       // cells per scan block (256 threads x 8)
 constexpr int kListCap = 32;          // grid engine, sparse cells: sorted neighbours kept per pass
-constexpr int kDenseMin = 12;         // boids in a cell for the CTA-per-cell path
+constexpr int kDenseMin = 12;         // default dense_min
+constexpr int kDeferMin = 4;          // smallest legal defer_min (and dense_min)
+constexpr int kCandDefer = 192;       // default cand_defer
+
+// Entries the dense-cell work list can need in one step: a full-size cell
+// (4 x cells) is listed at most once, by the scan when it holds dense_min
+// boids or by its first boid when it holds defer_min or more, both at least
+// kDeferMin.
+inline size_t dense_list_capacity(size_t ncell, size_t n)
+{
+    const size_t by_cells = ncell / 4, by_boids = n / kDeferMin;
+    return (by_cells < by_boids ? by_cells : by_boids) + 1;
+}
 constexpr int kDenseCap = 2048;       // candidates of a dense cell held in shared memory
-constexpr int kCandDefer = 192;       // a sparse cell with more candidates joins the dense path
 constexpr int kApCap = 64;            // all-pairs engine: neighbours kept per boid
 constexpr uint32_t kMaxBoids = 1u << 29;  // slot index packs into 29 bits
 
@@ -92,18 +131,40 @@ cudaError_t launch_pack(const float *pos3, const float *vel3, float4 *pos4, floa
                         uint32_t n, uint32_t *bad, float hi, cudaStream_t s, uint64_t *launches);
 cudaError_t launch_unpack(const float4 *pos4, const float4 *vel4, float *pos3, float *vel3,
                           uint32_t n, cudaStream_t s, uint64_t *launches);
+// One .ptcl frame in id order: pframe gets 3 floats per boid, or 12 with
+// forces (xyz + the nine get_force floats; zeros when force9 is null);
+// vframe (nullable) gets vx,vy,vz.
+cudaError_t launch_frame(const float4 *pos4, const float4 *vel4, const float *force9, float *pframe,
+                         float *vframe, int with_forces, uint32_t n, cudaStream_t s, uint64_t *launches);
+// ft == nullptr: one flock described by k; else a batched ensemble (k unused).
 cudaError_t launch_grid_keys(const StepConst &k, const float4 *pos, uint32_t *key, uint32_t *rank,
-                             uint32_t *count, cudaStream_t s, uint64_t *launches);
+                             uint32_t *count, cudaStream_t s, uint64_t *launches,
+                             const FlockTable *ft = nullptr);
 cudaError_t launch_grid_scan(const DevBuffers &b, cudaStream_t s, uint64_t *launches);
 cudaError_t launch_grid_scatter(const StepConst &k, const DevBuffers &b, int from, bool zero_counts,
-                                cudaStream_t s, uint64_t *launches);
+                                cudaStream_t s, uint64_t *launches, const FlockTable *ft = nullptr);
 // Rules + integration over the sorted state b.pos[from]; writes the new state
 // to b.pos[1-from] (diag == false) or neighbour-set fingerprints (diag == true).
 cudaError_t launch_grid_force(const StepConst &k, const DevBuffers &b, int from, bool diag,
-                              bool record_forces, cudaStream_t s, uint64_t *launches);
+                              bool record_forces, cudaStream_t s, uint64_t *launches,
+                              const FlockTable *ft = nullptr);
 cudaError_t launch_allpairs(const StepConst &k, const DevBuffers &b, int from, bool diag,
                             bool record_forces, cudaStream_t s, uint64_t *launches);
 cudaError_t launch_ref_cells(const StepConst &k, const float4 *pos, int32_t *cells8, cudaStream_t s,
                              uint64_t *launches);
+
+// Opt the dense-cell kernels in to their shared memory on the current device
+// (done before a stream capture, where it could not be).
+cudaError_t grid_prepare();
+
+// Ensemble statistics of the binned state b.pos[from] (see boids_kernels.cu):
+// acc gets kStatAcc doubles per flock, com 3 per flock, largest the largest
+// linked group per flock; link is the per-flock link distance; *err != 0
+// after the launch means a union-find walk hit its bound.  Uses b.key and
+// b.rank as scratch.
+constexpr int kStatAcc = 16;
+cudaError_t launch_ensemble_stats(const DevBuffers &b, int from, const FlockTable &ft, const float *link,
+                                  double *acc, double *com, uint32_t *largest, uint32_t *err, cudaStream_t s,
+                                  uint64_t *launches);
 
 }  // namespace boidsgpu

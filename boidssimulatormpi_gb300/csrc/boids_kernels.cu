@@ -275,6 +275,24 @@ __device__ __forceinline__ uint32_t cell_start(const uint32_t *__restrict__ lsta
     return __ldg(lstart + c) + __ldg(bsum + c / kScanTile);
 }
 
+// First state slot of global cell c of the flock described by k.
+__device__ __forceinline__ uint32_t slot_start(const uint32_t *__restrict__ lstart,
+                                               const uint32_t *__restrict__ bsum, uint32_t c, const StepConst &k)
+{
+    return cell_start(lstart, bsum, c) + k.slot_off;
+}
+
+// The constants of the flock that owns block blk of kSlotAlign slots, copied
+// into shared memory by the whole CTA (ends with a barrier).
+__device__ __forceinline__ void load_flock(StepConst &dst, const FlockTable &ft, uint32_t f)
+{
+    static_assert(sizeof(StepConst) % 4 == 0, "StepConst is copied as words");
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(ft.ks + f);
+    uint32_t *d = reinterpret_cast<uint32_t *>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(StepConst) / 4); i += blockDim.x) d[i] = __ldg(src + i);
+    __syncthreads();
+}
+
 // Where a rule kernel writes one boid's result.
 struct GridOut {
     float4 *pos_out, *vel_out;
@@ -288,7 +306,8 @@ template <bool DIAG>
 __device__ __forceinline__ void finish_boid(const Acc &a, float4 p4, float3 vi, uint32_t s, const GridOut &o,
                                             const StepConst &k)
 {
-    const uint32_t id = __float_as_uint(p4.w);
+    // output row of the boid: its id, after the boids of earlier flocks
+    const uint32_t id = __float_as_uint(p4.w) + (k.slot_base - k.slot_off);
     if (DIAG) {
         o.dcnt[3 * id + 0] = a.ncoh; o.dcnt[3 * id + 1] = a.nsep; o.dcnt[3 * id + 2] = a.nali;
         o.dhash[3 * id + 0] = a.h[0]; o.dhash[3 * id + 1] = a.h[1]; o.dhash[3 * id + 2] = a.h[2];
@@ -302,7 +321,7 @@ __device__ __forceinline__ void finish_boid(const Acc &a, float4 p4, float3 vi, 
     o.pos_out[s] = make_float4(x.x, x.y, x.z, p4.w);
     o.vel_out[s] = make_float4(v.x, v.y, v.z, 0.f);
     if (o.key_out) {  // binning for the next step
-        const uint32_t c = cell_key(x, k);
+        const uint32_t c = k.cell_base + cell_key(x, k);
         o.key_out[s] = c;
         o.rank_out[s] = atomicAdd(o.count + c, 1u);
     }
@@ -345,14 +364,42 @@ __global__ void k_unpack(const float4 *__restrict__ pos4, const float4 *__restri
     }
 }
 
-// ------------------------------------------------------------------ counting-sort binning
-
-__global__ void k_grid_keys(const float4 *__restrict__ pos, uint32_t *__restrict__ key,
-                            uint32_t *__restrict__ rank, uint32_t *__restrict__ count, StepConst k)
+// One output frame in the .ptcl layout of src/main.cpp:246-277: position
+// (+ get_force's nine floats) per boid, and optionally the velocity, both in
+// id order.  A thread per state slot; the scattered stores land in L2.
+__global__ void k_frame(const float4 *__restrict__ pos4, const float4 *__restrict__ vel4,
+                        const float *__restrict__ force9, float *__restrict__ pframe,
+                        float *__restrict__ vframe, int with_forces, uint32_t n)
 {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= k.n) return;
-    const uint32_t c = cell_key(xyz(pos[s]), k);
+    if (s >= n) return;
+    const float4 p = pos4[s];
+    const uint32_t id = __float_as_uint(p.w);
+    const size_t stride = with_forces ? 12 : 3;
+    float *o = pframe + stride * id;
+    o[0] = p.x; o[1] = p.y; o[2] = p.z;
+    if (with_forces) {
+        const float *f = force9 ? force9 + (size_t)9 * id : nullptr;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) o[3 + c] = f ? f[c] : 0.0f;
+    }
+    if (vframe) {
+        const float4 v = vel4[s];
+        vframe[(size_t)3 * id] = v.x; vframe[(size_t)3 * id + 1] = v.y; vframe[(size_t)3 * id + 2] = v.z;
+    }
+}
+
+// ------------------------------------------------------------------ counting-sort binning
+
+template <bool MULTI>
+__global__ void k_grid_keys(const float4 *__restrict__ pos, uint32_t *__restrict__ key,
+                            uint32_t *__restrict__ rank, uint32_t *__restrict__ count, StepConst kp, FlockTable ft)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= (MULTI ? ft.nslots : kp.n)) return;
+    const StepConst &k = MULTI ? ft.ks[ft.blk_flock[s / kSlotAlign]] : kp;
+    if (s - k.slot_base >= k.n) return;  // padding between flocks
+    const uint32_t c = k.cell_base + cell_key(xyz(pos[s]), k);
     key[s] = c;
     rank[s] = atomicAdd(count + c, 1u);
 }
@@ -361,7 +408,7 @@ __global__ void k_grid_keys(const float4 *__restrict__ pos, uint32_t *__restrict
 // kScanTile cells into lstart and publishes its total; the last block to
 // finish (completion ticket, no waiting) turns the totals into tile offsets
 // in bsum.  start(c) = lstart[c] + bsum[c / kScanTile].  Cells holding at
-// least kDenseMin boids are appended to the dense-cell work list.
+// least dense_min boids are appended to the dense-cell work list.
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = kScanTile / kScanThreads;  // 8
 
@@ -395,7 +442,8 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *warp_t
 
 __global__ void __launch_bounds__(kScanThreads)
 k_grid_scan(const uint32_t *__restrict__ count, uint32_t *__restrict__ lstart, uint32_t *bsum,
-            uint32_t *ticket, uint32_t nblocks, uint32_t *__restrict__ dense_list, uint32_t *dense_n)
+            uint32_t *ticket, uint32_t nblocks, uint32_t *__restrict__ dense_list, uint32_t *dense_n,
+            uint32_t dense_min)
 {
     __shared__ uint32_t warp_tot[kScanThreads / 32];
     __shared__ bool is_last;
@@ -407,8 +455,8 @@ k_grid_scan(const uint32_t *__restrict__ count, uint32_t *__restrict__ lstart, u
 #pragma unroll
     for (int i = 0; i < 8; ++i) sum += v[i];
     if (dense_list) {  // a full-size cell is 4 consecutive x cells; base is a multiple of 8
-        if (v[0] + v[1] + v[2] + v[3] >= (uint32_t)kDenseMin) dense_list[atomicAdd(dense_n, 1u)] = base / 4;
-        if (v[4] + v[5] + v[6] + v[7] >= (uint32_t)kDenseMin) dense_list[atomicAdd(dense_n, 1u)] = base / 4 + 1;
+        if (v[0] + v[1] + v[2] + v[3] >= dense_min) dense_list[atomicAdd(dense_n, 1u)] = base / 4;
+        if (v[4] + v[5] + v[6] + v[7] >= dense_min) dense_list[atomicAdd(dense_n, 1u)] = base / 4 + 1;
     }
     uint32_t total;
     uint32_t run = block_excl_scan<kScanThreads>(sum, warp_tot, total);
@@ -437,16 +485,25 @@ k_grid_scan(const uint32_t *__restrict__ count, uint32_t *__restrict__ lstart, u
     if (threadIdx.x == 0) *ticket = 0;  // ready for the next launch
 }
 
+template <bool MULTI>
 __global__ void k_grid_scatter(const float4 *__restrict__ pin, const float4 *__restrict__ vin,
                                const uint32_t *__restrict__ key, const uint32_t *__restrict__ rank,
                                const uint32_t *__restrict__ lstart, const uint32_t *__restrict__ bsum,
                                float4 *__restrict__ pout, float4 *__restrict__ vout,
-                               uint32_t *__restrict__ count_to_zero, uint32_t n)
+                               uint32_t *__restrict__ count_to_zero, uint32_t n, FlockTable ft)
 {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
+    uint32_t off = 0;
+    if (MULTI) {
+        if (s >= ft.nslots) return;
+        const StepConst &k = ft.ks[ft.blk_flock[s / kSlotAlign]];
+        if (s - k.slot_base >= k.n) return;
+        off = k.slot_off;
+    } else if (s >= n) {
+        return;
+    }
     const uint32_t c = key[s];
-    const uint32_t d = cell_start(lstart, bsum, c) + rank[s];
+    const uint32_t d = cell_start(lstart, bsum, c) + rank[s] + off;
     pout[d] = pin[s];
     vout[d] = vin[s];
     if (count_to_zero) count_to_zero[c] = 0;  // every binned cell, for the next step's keys
@@ -487,12 +544,9 @@ __device__ __forceinline__ Seg segment(int cx, int cy, int cz, int q, int runs, 
 // candidate list fits and either the cell is crowded or it holds a few boids
 // and its neighbourhood is crowded (then sorting once per cell beats sorting
 // per boid), else k_grid_sparse.
-constexpr int kDeferMin = 4;
-
-__device__ __forceinline__ bool dense_path(uint32_t b, uint32_t ncand)
+__device__ __forceinline__ bool dense_path(uint32_t b, uint32_t ncand, const StepConst &k)
 {
-    return ncand <= (uint32_t)kDenseCap &&
-           (b >= (uint32_t)kDenseMin || (b >= (uint32_t)kDeferMin && ncand > (uint32_t)kCandDefer));
+    return ncand <= (uint32_t)kDenseCap && (b >= k.dense_min || (b >= k.defer_min && ncand > k.cand_defer));
 }
 
 // ------------------------------------------------------------------ sparse cells: thread per boid
@@ -529,15 +583,20 @@ struct SparseSmem {
     uint64_t lst[kListA][kRT];   // accepted neighbours, sorted: id << 32 | slot | flags << 29
 };
 
-template <bool DIAG>
+template <bool DIAG, bool MULTI>
 __global__ void __launch_bounds__(kRT)
-k_grid_sparse(GridIn g, GridOut o, uint32_t *__restrict__ dense_list, uint32_t *__restrict__ dense_n, StepConst k)
+k_grid_sparse(GridIn g, GridOut o, uint32_t *__restrict__ dense_list, uint32_t *__restrict__ dense_n, StepConst kp,
+              FlockTable ft)
 {
+    static_assert(kRT == kSlotAlign, "a CTA serves one flock");
     __shared__ SparseSmem sm;
+    __shared__ StepConst kf;
+    if (MULTI) load_flock(kf, ft, ft.blk_flock[blockIdx.x]);
+    const StepConst &k = MULTI ? kf : kp;
     const int G = k.G, Gx = k.Gx;
     const int t = threadIdx.x;
     const uint32_t s = blockIdx.x * kRT + t;
-    bool act = s < k.n;
+    bool act = s - k.slot_base < k.n;
     const float4 p4 = act ? g.pos[s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 v4 = act ? g.vel[s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float3 pi = xyz(p4), vi = xyz(v4);
@@ -547,25 +606,26 @@ k_grid_sparse(GridIn g, GridOut o, uint32_t *__restrict__ dense_list, uint32_t *
         int zz = cz + r / 3 - 1, yy = cy + r % 3 - 1;
         zz = zz < 0 ? zz + G : (zz >= G ? zz - G : zz);
         yy = yy < 0 ? yy + G : (yy >= G ? yy - G : yy);
-        return (uint32_t)(zz * G + yy) * (uint32_t)Gx;
+        return k.cell_base + (uint32_t)(zz * G + yy) * (uint32_t)Gx;
     };
     if (act) {
         const uint32_t x0 = 4 * (uint32_t)cx, own_row = row_base(4);
-        const uint32_t own0 = cell_start(g.lstart, g.bsum, own_row + x0);
-        const uint32_t b = cell_start(g.lstart, g.bsum, own_row + x0 + 4) - own0;
-        if (b >= (uint32_t)kDeferMin) {
+        const uint32_t own0 = slot_start(g.lstart, g.bsum, own_row + x0, k);
+        const uint32_t b = slot_start(g.lstart, g.bsum, own_row + x0 + 4, k) - own0;
+        if (b >= k.defer_min) {
             // Which kernel: the count of the 27 full-size cells around the
             // boid's cell, exactly as k_grid_dense computes it.
             uint32_t ncell27 = 0;
             const int runs = seg_runs(cx, k);
             for (int q = 0; q < 9 * runs; ++q) {
                 const Seg sg = segment(cx, cy, cz, q, runs, k);
-                ncell27 += cell_start(g.lstart, g.bsum, sg.c1) - cell_start(g.lstart, g.bsum, sg.c0);
+                ncell27 += cell_start(g.lstart, g.bsum, k.cell_base + sg.c1) -
+                           cell_start(g.lstart, g.bsum, k.cell_base + sg.c0);
             }
-            if (dense_path(b, ncell27)) {
+            if (dense_path(b, ncell27, k)) {
                 // a crowded cell is listed by the scan; a cell with a crowded
                 // neighbourhood is listed here, once, by its first boid
-                if (b < (uint32_t)kDenseMin && s == own0)
+                if (b < k.dense_min && s == own0)
                     dense_list[atomicAdd(dense_n, 1u)] = own_row / 4 + (uint32_t)cx;
                 act = false;
             }
@@ -596,14 +656,14 @@ k_grid_sparse(GridIn g, GridOut o, uint32_t *__restrict__ dense_list, uint32_t *
             const uint32_t rb = row_base(r);
             const uint32_t rhi = (uint32_t)(r >> 3) << 31, rlo = (uint32_t)(r & 7) << 29;
             if (a1 > a0) {
-                const uint32_t j0 = cell_start(g.lstart, g.bsum, rb + a0), j1 = cell_start(g.lstart, g.bsum, rb + a1);
+                const uint32_t j0 = slot_start(g.lstart, g.bsum, rb + a0, k), j1 = slot_start(g.lstart, g.bsum, rb + a1, k);
                 sm.seg0[nseg][t] = j0 | (ca << 29) | rhi;
                 sm.seg1[nseg][t] = j1 | rlo;
                 ncand += j1 - j0;
                 ++nseg;
             }
             if (c1 > c0) {
-                const uint32_t j0 = cell_start(g.lstart, g.bsum, rb + c0), j1 = cell_start(g.lstart, g.bsum, rb + c1);
+                const uint32_t j0 = slot_start(g.lstart, g.bsum, rb + c0, k), j1 = slot_start(g.lstart, g.bsum, rb + c1, k);
                 sm.seg0[nseg][t] = j0 | (cb << 29) | rhi;
                 sm.seg1[nseg][t] = j1 | rlo;
                 ncand += j1 - j0;
@@ -752,7 +812,8 @@ struct DenseSmem {
     uint8_t ovf[kDT];
     uint32_t seg_j0[18], seg_k0[19];
     float seg_s[18][3];
-    uint32_t work;
+    uint32_t work, flock;
+    StepConst kf;  // the current cell's flock (batched ensembles)
 };
 static_assert(kDenseCap <= 2048, "gather index must fit 11 bits");
 
@@ -775,10 +836,10 @@ __device__ __forceinline__ float3 cand_image(float4 c, float3 pi, const float4 *
 // over in id order and the owner folds them in after its own, so the
 // accumulation order stays ascending id.  A chunk lane whose hand-over list
 // overflows leaves its chunk to the owner.
-template <bool DIAG>
+template <bool DIAG, bool MULTI>
 __global__ void __launch_bounds__(kDT, 4)
 k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint32_t *__restrict__ dense_n,
-             StepConst k)
+             StepConst kp, FlockTable ft)
 {
     extern __shared__ __align__(16) unsigned char dense_smem_raw[];
     DenseSmem &sm = *reinterpret_cast<DenseSmem *>(dense_smem_raw);
@@ -788,14 +849,28 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
         __syncthreads();
         const uint32_t w = sm.work;
         if (w >= dense_n[0]) break;
-        const uint32_t c = dense_list[w];
+        const uint32_t cg = dense_list[w];  // global full-size cell
+        if (MULTI) {
+            if (t == 0) {  // the flock: last with cell4 <= cg
+                uint32_t lo = 0, hi = ft.count;
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) / 2;
+                    if (__ldg(ft.cell4 + mid) <= cg) lo = mid; else hi = mid;
+                }
+                sm.flock = lo;
+            }
+            __syncthreads();
+            load_flock(sm.kf, ft, sm.flock);
+        }
+        const StepConst &k = MULTI ? sm.kf : kp;
+        const uint32_t c = cg - k.cell_base / 4;  // full-size cell inside the flock
         const int G = k.G;
         const int cx = (int)(c % G), cy = (int)((c / G) % G), cz = (int)(c / ((uint32_t)G * G));
         const int runs = seg_runs(cx, k), ns = 9 * runs;
         if (t < ns) {
             const Seg sg = segment(cx, cy, cz, t, runs, k);
-            sm.seg_j0[t] = cell_start(g.lstart, g.bsum, sg.c0);
-            sm.seg_k0[t + 1] = cell_start(g.lstart, g.bsum, sg.c1) - sm.seg_j0[t];  // length for now
+            sm.seg_j0[t] = slot_start(g.lstart, g.bsum, k.cell_base + sg.c0, k);
+            sm.seg_k0[t + 1] = slot_start(g.lstart, g.bsum, k.cell_base + sg.c1, k) - sm.seg_j0[t];  // length for now
             sm.seg_s[t][0] = sg.sx; sm.seg_s[t][1] = sg.sy; sm.seg_s[t][2] = sg.sz;
         }
         __syncthreads();
@@ -805,9 +880,9 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
         }
         __syncthreads();
         const uint32_t ncand = sm.seg_k0[ns];
-        const uint32_t own0 = cell_start(g.lstart, g.bsum, 4 * c);
-        const uint32_t b = cell_start(g.lstart, g.bsum, 4 * c + 4) - own0;
-        if (!dense_path(b, ncand)) {  // too many candidates: left to k_grid_sparse
+        const uint32_t own0 = slot_start(g.lstart, g.bsum, 4 * cg, k);
+        const uint32_t b = slot_start(g.lstart, g.bsum, 4 * cg + 4, k) - own0;
+        if (!dense_path(b, ncand, k)) {  // too many candidates: left to k_grid_sparse
             __syncthreads();
             continue;
         }
@@ -1097,11 +1172,22 @@ cudaError_t launch_unpack(const float4 *pos4, const float4 *vel4, float *pos3, f
     return cudaGetLastError();
 }
 
-cudaError_t launch_grid_keys(const StepConst &k, const float4 *pos, uint32_t *key, uint32_t *rank,
-                             uint32_t *count, cudaStream_t st, uint64_t *launches)
+cudaError_t launch_frame(const float4 *pos4, const float4 *vel4, const float *force9, float *pframe,
+                         float *vframe, int with_forces, uint32_t n, cudaStream_t st, uint64_t *launches)
 {
-    if (k.n == 0) return cudaSuccess;
-    k_grid_keys<<<blocks_for(k.n, 256), 256, 0, st>>>(pos, key, rank, count, k);
+    if (n == 0) return cudaSuccess;
+    k_frame<<<blocks_for(n, 256), 256, 0, st>>>(pos4, vel4, force9, pframe, vframe, with_forces, n);
+    ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grid_keys(const StepConst &k, const float4 *pos, uint32_t *key, uint32_t *rank,
+                             uint32_t *count, cudaStream_t st, uint64_t *launches, const FlockTable *ft)
+{
+    const uint32_t n = ft ? ft->nslots : k.n;
+    if (n == 0) return cudaSuccess;
+    if (ft) k_grid_keys<true><<<blocks_for(n, 256), 256, 0, st>>>(pos, key, rank, count, k, *ft);
+    else k_grid_keys<false><<<blocks_for(n, 256), 256, 0, st>>>(pos, key, rank, count, k, FlockTable{});
     ++*launches;
     return cudaGetLastError();
 }
@@ -1111,26 +1197,65 @@ cudaError_t launch_grid_scan(const DevBuffers &b, cudaStream_t st, uint64_t *lau
     cudaError_t e = cudaMemsetAsync(b.dense_n, 0, 2 * sizeof(uint32_t), st);  // count, work queue
     if (e != cudaSuccess) return e;
     k_grid_scan<<<b.nscan_blocks, kScanThreads, 0, st>>>(b.count, b.lstart, b.bsum, b.ticket, b.nscan_blocks,
-                                                          b.dense_list, b.dense_n);
+                                                          b.dense_list, b.dense_n, b.dense_min);
     ++*launches;
     return cudaGetLastError();
 }
 
 cudaError_t launch_grid_scatter(const StepConst &k, const DevBuffers &b, int from, bool zero_counts,
-                                cudaStream_t st, uint64_t *launches)
+                                cudaStream_t st, uint64_t *launches, const FlockTable *ft)
 {
-    if (k.n == 0) return cudaSuccess;
-    k_grid_scatter<<<blocks_for(k.n, 256), 256, 0, st>>>(b.pos[from], b.vel[from], b.key, b.rank, b.lstart,
-                                                         b.bsum, b.pos[1 - from], b.vel[1 - from],
-                                                         zero_counts ? b.count : nullptr, k.n);
+    const uint32_t n = ft ? ft->nslots : k.n;
+    if (n == 0) return cudaSuccess;
+    uint32_t *cz = zero_counts ? b.count : nullptr;
+    if (ft)
+        k_grid_scatter<true><<<blocks_for(n, 256), 256, 0, st>>>(b.pos[from], b.vel[from], b.key, b.rank, b.lstart,
+                                                                 b.bsum, b.pos[1 - from], b.vel[1 - from], cz, n, *ft);
+    else
+        k_grid_scatter<false><<<blocks_for(n, 256), 256, 0, st>>>(b.pos[from], b.vel[from], b.key, b.rank, b.lstart,
+                                                                  b.bsum, b.pos[1 - from], b.vel[1 - from], cz, n,
+                                                                  FlockTable{});
     ++*launches;
     return cudaGetLastError();
 }
 
-cudaError_t launch_grid_force(const StepConst &k, const DevBuffers &b, int from, bool diag, bool record_forces,
-                              cudaStream_t st, uint64_t *launches)
+namespace {
+
+// The dense kernel's shared memory exceeds the 48 KB default: opt in once
+// per device and instantiation.
+template <bool DIAG, bool MULTI>
+cudaError_t dense_smem_opt_in()
 {
-    if (k.n == 0) return cudaSuccess;
+    static uint64_t done = 0;  // bit per device ordinal
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev < 64 ? 1ull << dev : 0;
+    if (bit && (__atomic_load_n(&done, __ATOMIC_ACQUIRE) & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(k_grid_dense<DIAG, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(DenseSmem));
+    if (e == cudaSuccess && bit) __atomic_fetch_or(&done, bit, __ATOMIC_RELEASE);
+    return e;
+}
+
+template <bool DIAG, bool MULTI>
+cudaError_t grid_force(const StepConst &k, const GridIn &g, const GridOut &o, const DevBuffers &b, unsigned nsp,
+                       const FlockTable &ft, cudaStream_t st)
+{
+    cudaError_t e = dense_smem_opt_in<DIAG, MULTI>();
+    if (e != cudaSuccess) return e;
+    k_grid_sparse<DIAG, MULTI><<<nsp, kRT, 0, st>>>(g, o, b.dense_list, b.dense_n, k, ft);
+    k_grid_dense<DIAG, MULTI><<<b.dense_grid, kDT, sizeof(DenseSmem), st>>>(g, o, b.dense_list, b.dense_n, k, ft);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_grid_force(const StepConst &k, const DevBuffers &b, int from, bool diag, bool record_forces,
+                              cudaStream_t st, uint64_t *launches, const FlockTable *ft)
+{
+    const uint32_t n = ft ? ft->nslots : k.n;
+    if (n == 0) return cudaSuccess;
     GridIn g{b.pos[from], b.vel[from], b.lstart, b.bsum};
     GridOut o{};
     if (diag) {
@@ -1144,25 +1269,13 @@ cudaError_t launch_grid_force(const StepConst &k, const DevBuffers &b, int from,
         o.count = b.count;
         o.forces = record_forces ? b.forces : nullptr;
     }
-    const unsigned nsp = blocks_for(k.n, kRT);
-    const unsigned nd = b.dense_grid;
-    const size_t dsm = sizeof(DenseSmem);
-    static bool attr_set[2] = {false, false};
-    if (!attr_set[diag]) {
-        cudaError_t e = diag ? cudaFuncSetAttribute(k_grid_dense<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm)
-                             : cudaFuncSetAttribute(k_grid_dense<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
-        if (e != cudaSuccess) return e;
-        attr_set[diag] = true;
-    }
-    if (diag) {
-        k_grid_sparse<true><<<nsp, kRT, 0, st>>>(g, o, b.dense_list, b.dense_n, k);
-        k_grid_dense<true><<<nd, kDT, dsm, st>>>(g, o, b.dense_list, b.dense_n, k);
-    } else {
-        k_grid_sparse<false><<<nsp, kRT, 0, st>>>(g, o, b.dense_list, b.dense_n, k);
-        k_grid_dense<false><<<nd, kDT, dsm, st>>>(g, o, b.dense_list, b.dense_n, k);
-    }
-    *launches += 2;
-    return cudaGetLastError();
+    const unsigned nsp = blocks_for(n, kRT);
+    const FlockTable none{};
+    cudaError_t e;
+    if (ft) e = diag ? grid_force<true, true>(k, g, o, b, nsp, *ft, st) : grid_force<false, true>(k, g, o, b, nsp, *ft, st);
+    else e = diag ? grid_force<true, false>(k, g, o, b, nsp, none, st) : grid_force<false, false>(k, g, o, b, nsp, none, st);
+    if (e == cudaSuccess) *launches += 2;
+    return e;
 }
 
 cudaError_t launch_allpairs(const StepConst &k, const DevBuffers &b, int from, bool diag, bool record_forces,
@@ -1200,6 +1313,219 @@ cudaError_t launch_ref_cells(const StepConst &k, const float4 *pos, int32_t *cel
     k_ref_cells<<<blocks_for(k.n, 256), 256, 0, st>>>(pos, cells8, k);
     ++*launches;
     return cudaGetLastError();
+}
+
+
+// ------------------------------------------------------------------ ensemble statistics
+//
+// Order statistics of every flock of a batched ensemble, on a freshly binned
+// state (sorted slots, valid cell tables).  Sums are FP64.  Per flock the
+// accumulator holds kStatAcc doubles:
+//   0-2  sum of unit velocities        3-5  sum of velocities
+//   6-8  sum of sin(2 pi x / F)        9-11 sum of cos(2 pi x / F)
+//   12-14 sum of r_hat x v_hat (about the centre of mass)
+//   15   sum of capped nearest-neighbour distances
+namespace {
+
+constexpr int kStatThreads = kSlotAlign;
+constexpr uint32_t kFindCap = 1u << 24;  // bound on union-find walks (far above any tree height)
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-reduce NV doubles per thread into acc[0..NV) with one atomic each.
+template <int NV>
+__device__ __forceinline__ void block_sum_to(const double (&v)[NV], double *acc)
+{
+    __shared__ double part[NV][kStatThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        const double s = warp_sum(v[i]);
+        if (lane == 0) part[i][w] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < kStatThreads / 32; ++q) s += part[threadIdx.x][q];
+        atomicAdd(acc + threadIdx.x, s);
+    }
+}
+
+__device__ __forceinline__ uint32_t uf_find(const uint32_t *parent, uint32_t x, uint32_t *err)
+{
+    for (uint32_t it = 0; it < kFindCap; ++it) {
+        const uint32_t p = __ldcg(parent + x);
+        if (p == x) return x;
+        x = p;
+    }
+    atomicOr(err, 1u);
+    return x;
+}
+
+// Lock-free union: hook the larger root under the smaller one; a failed CAS
+// means that root was hooked meanwhile, so retry from the new roots.
+__device__ __forceinline__ void uf_union(uint32_t *parent, uint32_t a, uint32_t b, uint32_t *err)
+{
+    for (uint32_t it = 0; it < kFindCap; ++it) {
+        a = uf_find(parent, a, err);
+        b = uf_find(parent, b, err);
+        if (a == b) return;
+        const uint32_t hi = a > b ? a : b, lo = a > b ? b : a;
+        const uint32_t old = atomicCAS(parent + hi, hi, lo);
+        if (old == hi) return;
+        a = lo;
+        b = old;
+    }
+    atomicOr(err, 2u);
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kStatThreads)
+k_stat_moments(const float4 *__restrict__ pos, const float4 *__restrict__ vel, FlockTable ft, double *acc,
+               uint32_t *__restrict__ parent)
+{
+    __shared__ StepConst kf;
+    load_flock(kf, ft, ft.blk_flock[blockIdx.x]);
+    const uint32_t s = blockIdx.x * kStatThreads + threadIdx.x;
+    parent[s] = s;
+    double v[12] = {};
+    if (s - kf.slot_base < kf.n) {
+        const float4 p = pos[s], u = vel[s];
+        const double vx = u.x, vy = u.y, vz = u.z;
+        const double sp = sqrt(vx * vx + vy * vy + vz * vz);
+        if (sp > 0.0) { v[0] = vx / sp; v[1] = vy / sp; v[2] = vz / sp; }
+        v[3] = vx; v[4] = vy; v[5] = vz;
+        const double inv = 2.0 / kf.F;
+        sincospi(p.x * inv, &v[6], &v[9]);
+        sincospi(p.y * inv, &v[7], &v[10]);
+        sincospi(p.z * inv, &v[8], &v[11]);
+    }
+    block_sum_to<12>(v, acc + (size_t)kf.flock * kStatAcc);
+}
+
+// Centre of mass per flock: the periodic (circular) mean on each axis.
+__global__ void k_stat_com(const double *__restrict__ acc, const StepConst *__restrict__ ks, uint32_t count,
+                           double *__restrict__ com)
+{
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= count) return;
+    const double *a = acc + (size_t)f * kStatAcc;
+    const double F = ks[f].F;
+    for (int d = 0; d < 3; ++d) {
+        double c = atan2(a[6 + d], a[9 + d]) / (2.0 * 3.141592653589793) * F;
+        if (c < 0.0) c += F;
+        com[3 * f + d] = c;
+    }
+}
+
+// Milling sum, capped nearest-neighbour distances and the union of every
+// pair nearer than the link distance (the flock's cohesion sight distance),
+// over the 27 full-size cells around each boid.
+__global__ void __launch_bounds__(kStatThreads)
+k_stat_pairs(GridIn g, FlockTable ft, const double *__restrict__ com, const float *__restrict__ link,
+             double *acc, uint32_t *parent, uint32_t *err)
+{
+    __shared__ StepConst kf;
+    load_flock(kf, ft, ft.blk_flock[blockIdx.x]);
+    const StepConst &k = kf;
+    const uint32_t s = blockIdx.x * kStatThreads + threadIdx.x;
+    double v[4] = {};
+    if (s - k.slot_base < k.n) {
+        const float4 p4 = g.pos[s], u = g.vel[s];
+        const float3 pi = xyz(p4);
+        // r_hat x v_hat about the periodic centre of mass
+        double r[3] = {pi.x - com[3 * k.flock], pi.y - com[3 * k.flock + 1], pi.z - com[3 * k.flock + 2]};
+        for (int d = 0; d < 3; ++d) {
+            if (r[d] > 0.5 * k.F) r[d] -= k.F;
+            else if (r[d] < -0.5 * k.F) r[d] += k.F;
+        }
+        const double rn = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+        const double vx = u.x, vy = u.y, vz = u.z;
+        const double sp = sqrt(vx * vx + vy * vy + vz * vz);
+        if (rn > 0.0 && sp > 0.0) {
+            const double a0 = r[0] / rn, a1 = r[1] / rn, a2 = r[2] / rn;
+            const double b0 = vx / sp, b1 = vy / sp, b2 = vz / sp;
+            v[0] = a1 * b2 - a2 * b1;
+            v[1] = a2 * b0 - a0 * b2;
+            v[2] = a0 * b1 - a1 * b0;
+        }
+        const int cx = cell1(pi.x, k), cy = cell1(pi.y, k), cz = cell1(pi.z, k);
+        const int runs = seg_runs(cx, k);
+        const float lk = link[k.flock];
+        float nn2 = k.side * k.side;
+        for (int q = 0; q < 9 * runs; ++q) {
+            const Seg sg = segment(cx, cy, cz, q, runs, k);
+            const uint32_t j0 = slot_start(g.lstart, g.bsum, k.cell_base + sg.c0, k);
+            const uint32_t j1 = slot_start(g.lstart, g.bsum, k.cell_base + sg.c1, k);
+            for (uint32_t j = j0; j < j1; ++j) {
+                if (j == s) continue;
+                const float4 pj = __ldg(g.pos + j);
+                const float dx = pj.x + sg.sx - pi.x, dy = pj.y + sg.sy - pi.y, dz = pj.z + sg.sz - pi.z;
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                nn2 = fminf(nn2, d2);
+                if (j > s && d2 < lk * lk) uf_union(parent, s, j, err);
+            }
+        }
+        v[3] = sqrt((double)nn2);
+    }
+    block_sum_to<4>(v, acc + (size_t)k.flock * kStatAcc + 12);
+}
+
+// Component sizes: every boid adds one to its root's count.
+__global__ void k_stat_roots(FlockTable ft, const uint32_t *parent, uint32_t *__restrict__ size, uint32_t *err)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= ft.nslots) return;
+    const StepConst &k = ft.ks[ft.blk_flock[s / kSlotAlign]];
+    if (s - k.slot_base >= k.n) return;
+    atomicAdd(size + uf_find(parent, s, err), 1u);
+}
+
+__global__ void k_stat_largest(FlockTable ft, const uint32_t *__restrict__ parent, const uint32_t *__restrict__ size,
+                               uint32_t *__restrict__ largest)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= ft.nslots) return;
+    const StepConst &k = ft.ks[ft.blk_flock[s / kSlotAlign]];
+    if (s - k.slot_base >= k.n || parent[s] != s) return;
+    atomicMax(largest + k.flock, size[s]);
+}
+
+cudaError_t launch_ensemble_stats(const DevBuffers &b, int from, const FlockTable &ft, const float *link,
+                                  double *acc, double *com, uint32_t *largest, uint32_t *err, cudaStream_t st,
+                                  uint64_t *launches)
+{
+    const unsigned nb = ft.nslots / kStatThreads;
+    uint32_t *parent = b.key, *size = b.rank;  // free between a step's binning and its rule pass
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(acc, 0, sizeof(double) * kStatAcc * ft.count, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(largest, 0, sizeof(uint32_t) * ft.count, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(size, 0, sizeof(uint32_t) * ft.nslots, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(err, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+    k_stat_moments<<<nb, kStatThreads, 0, st>>>(b.pos[from], b.vel[from], ft, acc, parent);
+    k_stat_com<<<blocks_for(ft.count, 128), 128, 0, st>>>(acc, ft.ks, ft.count, com);
+    GridIn g{b.pos[from], b.vel[from], b.lstart, b.bsum};
+    k_stat_pairs<<<nb, kStatThreads, 0, st>>>(g, ft, com, link, acc, parent, err);
+    k_stat_roots<<<blocks_for(ft.nslots, 256), 256, 0, st>>>(ft, parent, size, err);
+    k_stat_largest<<<blocks_for(ft.nslots, 256), 256, 0, st>>>(ft, parent, size, largest);
+    *launches += 5;
+    return cudaGetLastError();
+}
+
+cudaError_t grid_prepare()
+{
+    cudaError_t e;
+    if ((e = dense_smem_opt_in<false, false>()) != cudaSuccess) return e;
+    if ((e = dense_smem_opt_in<true, false>()) != cudaSuccess) return e;
+    if ((e = dense_smem_opt_in<false, true>()) != cudaSuccess) return e;
+    return dense_smem_opt_in<true, true>();
 }
 
 }  // namespace boidsgpu

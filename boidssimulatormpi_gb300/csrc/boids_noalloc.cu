@@ -70,7 +70,7 @@ size_t layout(const boidsgpu::StepConst &k, unsigned char *base, boidsgpu::DevBu
     b->ncell = (uint32_t)k.Gx * k.G * k.G;
     b->ncell_pad = (b->ncell + 1 + boidsgpu::kScanTile - 1) / boidsgpu::kScanTile * boidsgpu::kScanTile;
     b->nscan_blocks = b->ncell_pad / boidsgpu::kScanTile;
-    const size_t ndense = (b->ncell < n / boidsgpu::kDenseMin ? b->ncell : n / boidsgpu::kDenseMin) + 1;
+    const size_t ndense = boidsgpu::dense_list_capacity(b->ncell, n);
     size_t off = 0;
     auto take = [&](size_t bytes) {
         unsigned char *p = base ? base + off : nullptr;
@@ -124,6 +124,7 @@ extern "C" int boids_step_noalloc(const boids_params *params, const float *pos3n
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, params->device);
     b.dense_grid = (uint32_t)(nsm > 0 ? nsm : 1) * 4;
+    b.dense_min = k.dense_min;
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     uint64_t launches = 0;
     // the array keeps the previous call's contents: clear what must start at zero

@@ -159,6 +159,90 @@ int boids_profile_read(boids_sim *sim, boids_profile_t *out, int32_t reset);
 /* Number of this library's kernels launched by the handle so far. */
 uint64_t boids_kernel_launches(boids_sim *sim);
 
+/* .ptcl frame output: replaces the per-boid get()/get_v()/get_force() loop
+ * of the reference's frame writer (src/main.cpp:246-277).  Queues on the
+ * handle's stream the assembly of one frame of the current state, in the
+ * byte layout main.cpp writes, and its copy into host memory:
+ *   pos_frame  x,y,z per boid in id order (3 floats), or with
+ *              with_forces != 0 (--force-data-output) x,y,z followed by
+ *              get_force's nine floats of the last step (12 floats per
+ *              boid); the forces are zero before the first step, as the
+ *              reference's zero-initialised dv arrays are;
+ *   vel_frame  vx,vy,vz per boid (--velocity-output), nullable.
+ * On a little-endian host these are the bytes fix_byte_order passes through
+ * unchanged (src/main.cpp:26-36).  The call returns without waiting; the
+ * frame has landed once boids_frame_wait(sim, slot) returns.  slot
+ * (0 .. BOIDS_FRAME_SLOTS-1) names the completion event, so that frames can
+ * be double-buffered while the next update runs.  Host buffers from
+ * boids_host_alloc (page-locked) let the copy overlap the GPU work. */
+#define BOIDS_FRAME_SLOTS 4
+int boids_frame_async(boids_sim *sim, float *pos_frame, float *vel_frame, int32_t with_forces,
+                      int32_t slot);
+
+/* Wait for frame slot's copies.  It only waits on a CUDA event, so a writer
+ * thread may call it while another thread queues the next update. */
+int boids_frame_wait(boids_sim *sim, int32_t slot);
+
+/* Page-locked host memory (cudaHostAlloc) for frame buffers; no counterpart
+ * in the reference, which writes from its AoS boid array. */
+int boids_host_alloc(size_t bytes, void **out);
+void boids_host_free(void *p);
+
+/* ------------------------------------------------------------------ ensembles
+ *
+ * A batched ensemble: many independent grid-engine flocks of uneven size,
+ * each with its own parameters, stepped together by one launch per kernel
+ * per step (the steps replayed from a captured CUDA graph).  No counterpart
+ * in the reference, whose executables run one flock per process; every
+ * flock's trajectory is bit-identical to a boids_create(BOIDS_ENGINE_GRID)
+ * handle with the same parameters and initial state. */
+typedef struct boids_ensemble boids_ensemble;
+
+#define BOIDS_INIT_RANDOM_UNIFORM 0
+#define BOIDS_INIT_TEST 1
+
+typedef struct {
+    boids_params params;  /* engine must be BOIDS_ENGINE_GRID; device and flags are taken from flock 0 */
+    int32_t init_kind;    /* BOIDS_INIT_*: the drawn placements of BoidSimulation::init */
+    int32_t rand_seed;    /* srand48 seed, as the grid engine's init uses it */
+} boids_flock_desc;
+
+/* Per-flock statistics written by boids_ensemble_stats, in this order. */
+#define BOIDS_STAT_POLARIZATION 0  /* |sum of unit velocities| / N                      */
+#define BOIDS_STAT_MILLING 1       /* |sum of r_hat x v_hat| / N about the centre of mass */
+#define BOIDS_STAT_NN_DISTANCE 2   /* mean nearest-neighbour distance, capped at the search radius */
+#define BOIDS_STAT_LARGEST_CLUSTER 3  /* largest linked group / N (link: cohesion sight distance) */
+#define BOIDS_STAT_COM_X 4         /* centre of mass, periodic (circular) mean, FP64       */
+#define BOIDS_STAT_COM_Y 5
+#define BOIDS_STAT_COM_Z 6
+#define BOIDS_STAT_MOMENTUM_X 7    /* mean velocity (momentum per boid), FP64              */
+#define BOIDS_STAT_MOMENTUM_Y 8
+#define BOIDS_STAT_MOMENTUM_Z 9
+#define BOIDS_STAT_SEARCH_RADIUS 10 /* the cap of the nearest-neighbour search             */
+#define BOIDS_STATS_PER_FLOCK 11
+
+int boids_ensemble_create(const boids_flock_desc *flocks, uint32_t count, boids_ensemble **out);
+void boids_ensemble_destroy(boids_ensemble *ens);
+/* BoidSimulation::init of every flock (grid engine: srand48(rand_seed)). */
+int boids_ensemble_init(boids_ensemble *ens);
+/* Replace one flock's state (id order, 3 floats per boid). */
+int boids_ensemble_set_state(boids_ensemble *ens, uint32_t flock, const float *pos3n, const float *vel3n);
+/* `steps` updates of every flock.  Asynchronous on the ensemble's stream. */
+int boids_ensemble_step(boids_ensemble *ens, int32_t steps);
+/* One flock's state in id order.  Synchronous. */
+int boids_ensemble_get_state(boids_ensemble *ens, uint32_t flock, float *pos3n, float *vel3n);
+/* BOIDS_STATS_PER_FLOCK doubles per flock for the current state.  Synchronous. */
+int boids_ensemble_stats(boids_ensemble *ens, double *out);
+/* Time a few steps with each candidate of the dense-cell thresholds (which
+ * cells take the CTA-per-cell kernel) on a copy of the current state and
+ * keep the fastest; results do not depend on the choice.  steps_per_trial
+ * <= 0 picks a default.  Leaves the state as it was. */
+int boids_ensemble_autotune(boids_ensemble *ens, int32_t steps_per_trial);
+/* Chosen thresholds: dense_min, defer_min, cand_defer. */
+int boids_ensemble_tuning(boids_ensemble *ens, int32_t *out3);
+int boids_ensemble_synchronize(boids_ensemble *ens);
+uint64_t boids_ensemble_kernel_launches(boids_ensemble *ens);
+
 /* Scratch reserved by boids_step_noalloc on every GPU that loads the library. */
 #define BOIDS_NOALLOC_SCRATCH_BYTES (32u << 20)
 

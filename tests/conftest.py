@@ -58,3 +58,16 @@ def assert_bits_equal(a, b, what=""):
         idx = np.nonzero(diff)[0]
         raise AssertionError("%s: %d of %d values differ; first at %d: %r vs %r"
                              % (what, idx.size, a.size, idx[0], a[idx[0]], b[idx[0]]))
+
+
+@pytest.fixture(scope="session")
+def cli(boids_lib):
+    """Paths of the boidsim / boidsim_grid executables (built with the library)."""
+    from boidssimulatormpi_gb300 import build as bld
+    paths = {name: os.path.join(bld.BIN, name) for name in ("boidsim", "boidsim_grid")}
+    for p in paths.values():
+        assert os.access(p, os.X_OK), p
+    return paths
+
+
+DATA = os.path.join(ROOT, "tests", "data")
