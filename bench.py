@@ -60,6 +60,9 @@ def parse():
                     help="untimed steps before the supplementary clustered-regime timing (0: skip)")
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ensemble-flocks", type=int, default=256,
+                    help="supplementary batched-ensemble sweep (0: skip)")
+    ap.add_argument("--ensemble-steps", type=int, default=2000)
     return ap.parse_args()
 
 
@@ -198,6 +201,54 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ ensemble sweep
+
+def ensemble_flocks(B, count, seed):
+    """The batched-ensemble sweep: each flock's N log-uniform in [2^10, 2^16],
+    F keeping the density of 16384 boids per unit volume, and the marun2019
+    radii, weights and vmax each scaled by a factor uniform in [0.7, 1.3]."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    m = MARUN2019
+    flocks, total = [], 0
+    for i in range(count):
+        n = int(round(2 ** rng.uniform(10, 16)))
+        f = rng.uniform(0.7, 1.3, 7)
+        F = (n / 16384.0) ** (1.0 / 3.0)
+        sep = (m["sep"][0] * f[0], m["sep"][1], m["sep"][2] * f[3])
+        ali = (m["ali"][0] * f[1], m["ali"][1], m["ali"][2] * f[4])
+        coh = (m["coh"][0] * f[2], m["coh"][1], m["coh"][2] * f[5])
+        flocks.append((B.flock_params(n, F, sep, ali, coh, m["vmax"] * f[6], m["vmin"]),
+                       B.INIT_RANDOM_UNIFORM, seed + i))
+        total += n
+    return flocks, total
+
+
+def run_ensemble(a, B, rank, dist):
+    """Sweep time of the whole ensemble for --ensemble-steps steps (after
+    autotuning on the initial state), with the per-flock statistics at the end."""
+    import numpy as np
+    flocks, total = ensemble_flocks(B, a.ensemble_flocks, 2024 + 1000 * rank)
+    ens = B.Ensemble(flocks)
+    ens.init()
+    tuning = ens.autotune()
+    ens.step(3)  # warm-up, graph capture
+    ens.synchronize()
+    t0 = time.perf_counter()
+    ens.step(a.ensemble_steps)
+    ens.synchronize()
+    dt, units = reduce_over_ranks(dist, time.perf_counter() - t0, float(total * a.ensemble_steps))
+    st = ens.stats()
+    launches = ens.kernel_launches()
+    ens.close()
+    return {"flocks": a.ensemble_flocks, "boids": total, "steps": a.ensemble_steps,
+            "sweep_s": dt, "ms_per_step": dt * 1e3 / a.ensemble_steps,
+            "boid_steps_per_s": units / dt, "tuning": list(tuning), "kernel_launches": launches,
+            "stats_mean": {k: float(np.mean(st[:, i])) for i, k in enumerate(B.STAT_NAMES[:4])},
+            "config": "N log-uniform in [2^10, 2^16], F = (N/16384)^(1/3), marun2019 radii, weights "
+                      "and vmax x U[0.7, 1.3], random_uniform init, steps replayed from CUDA graphs"}
+
+
 # ------------------------------------------------------------------ our arm
 
 def cpu_baseline_sample(a, pos, vel):
@@ -315,8 +366,9 @@ def run_ours(a):
         late = {"after_steps": a.warmup + a.late_presteps, "ms_per_step": sum(ms) / len(ms),
                 "value": a.n * len(ms) / (sum(ms) / 1e3), "unit": UNIT}
 
+    sim.close()
+    ens = run_ensemble(a, B, rank, dist) if a.ensemble_flocks > 0 else None
     if rank != 0:
-        sim.close()
         return
     peaks = {}
     try:
@@ -353,9 +405,8 @@ def run_ours(a):
             "config": dict(workload(a), l2="flushed before every timed step (256 MiB write)",
                            parallelism="replicas" if ws > 1 else "single GPU"),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk.summary(), "late_regime": late,
+            "clocks": clk.summary(), "late_regime": late, "ensemble": ens,
             "step_ms_min_max": [min(step_ms), max(step_ms)]}
-    sim.close()
     print(json.dumps(line), flush=True)
 
 

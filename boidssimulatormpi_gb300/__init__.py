@@ -75,6 +75,8 @@ SIGNATURES = {
     "boids_profile_enable": (C.c_int, [_vp, C.c_int32]),
     "boids_profile_read": (C.c_int, [_vp, C.POINTER(Profile), C.c_int32]),
     "boids_kernel_launches": (C.c_uint64, [_vp]),
+    "boids_set_tuning": (C.c_int, [_vp, _vp]),
+    "boids_get_tuning": (C.c_int, [_vp, _vp]),
     "boids_frame_async": (C.c_int, [_vp, _vp, _vp, C.c_int32, C.c_int32]),
     "boids_frame_wait": (C.c_int, [_vp, C.c_int32]),
     "boids_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_vp)]),
@@ -90,6 +92,15 @@ SIGNATURES = {
     "boids_ensemble_tuning": (C.c_int, [_vp, _vp]),
     "boids_ensemble_synchronize": (C.c_int, [_vp]),
     "boids_ensemble_kernel_launches": (C.c_uint64, [_vp]),
+    "boids_mlp_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_int32, C.POINTER(_vp)]),
+    "boids_mlp_destroy": (None, [_vp]),
+    "boids_mlp_param_count": (C.c_int64, [_vp]),
+    "boids_mlp_get_params": (C.c_int, [_vp, _vp]),
+    "boids_mlp_set_params": (C.c_int, [_vp, _vp]),
+    "boids_mlp_forward": (C.c_int, [_vp, _vp, C.c_int32, _vp]),
+    "boids_mlp_gradient": (C.c_int, [_vp, _vp, _vp, C.c_int32, _vp, C.POINTER(C.c_double)]),
+    "boids_mlp_train": (C.c_int, [_vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_uint64,
+                                  C.POINTER(C.c_double)]),
     "boids_step_noalloc": (C.c_int, [C.POINTER(Params), _vp, _vp, _vp, _vp, _vp]),
     "boids_last_error": (C.c_char_p, []),
     "boids_version": (C.c_char_p, []),
@@ -255,6 +266,15 @@ class BoidSimulation:
         _, v = self._state_cached()
         return tuple(float(x) for x in v[i])
 
+    def set_tuning(self, dense_min, defer_min, cand_defer, lone_cand):
+        t = np.array([dense_min, defer_min, cand_defer, lone_cand], np.int32)
+        _check(lib().boids_set_tuning(self.h, _ptr(t)))
+
+    def tuning(self):
+        t = np.zeros(4, np.int32)
+        _check(lib().boids_get_tuning(self.h, _ptr(t)))
+        return tuple(int(x) for x in t)
+
     def get_force(self, i):
         return tuple(float(x) for x in self.forces()[i])
 
@@ -344,7 +364,7 @@ class Ensemble:
         return self.tuning()
 
     def tuning(self):
-        t = np.zeros(3, np.int32)
+        t = np.zeros(4, np.int32)
         _check(lib().boids_ensemble_tuning(self.h, _ptr(t)))
         return tuple(int(x) for x in t)
 
@@ -354,6 +374,63 @@ class Ensemble:
     def close(self):
         if self.h is not None and _lib is not None:
             _lib.boids_ensemble_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------ sweep surrogate
+
+class Surrogate:
+    """The BF16 tensor-core MLP of boids_mlp_* (in -> hidden -> hidden -> out)."""
+
+    def __init__(self, n_in=8, n_hidden=256, n_out=4, seed=1, device=0):
+        h = C.c_void_p()
+        _check(lib().boids_mlp_create(n_in, n_hidden, n_out, seed, device, C.byref(h)))
+        self.h = h
+        self.n_in, self.n_hidden, self.n_out = n_in, n_hidden, n_out
+
+    def param_count(self):
+        return int(lib().boids_mlp_param_count(self.h))
+
+    def params(self):
+        p = np.empty(self.param_count(), np.float32)
+        _check(lib().boids_mlp_get_params(self.h, _ptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = _f32(p, self.param_count())
+        _check(lib().boids_mlp_set_params(self.h, _ptr(p)))
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, self.n_in)
+        y = np.empty((x.shape[0], self.n_out), np.float32)
+        _check(lib().boids_mlp_forward(self.h, _ptr(x), x.shape[0], _ptr(y)))
+        return y
+
+    def gradient(self, x, t):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, self.n_in)
+        t = np.ascontiguousarray(t, np.float32).reshape(-1, self.n_out)
+        g = np.empty(self.param_count(), np.float32)
+        loss = C.c_double()
+        _check(lib().boids_mlp_gradient(self.h, _ptr(x), _ptr(t), x.shape[0], _ptr(g), C.byref(loss)))
+        return g, loss.value
+
+    def train(self, x, t, epochs=200, batch=256, lr=1e-3, seed=7):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, self.n_in)
+        t = np.ascontiguousarray(t, np.float32).reshape(-1, self.n_out)
+        loss = C.c_double()
+        _check(lib().boids_mlp_train(self.h, _ptr(x), _ptr(t), x.shape[0], epochs, batch, lr, seed,
+                                     C.byref(loss)))
+        return loss.value
+
+    def close(self):
+        if self.h is not None and _lib is not None:
+            _lib.boids_mlp_destroy(self.h)
         self.h = None
 
     def __del__(self):

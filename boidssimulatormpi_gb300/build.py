@@ -71,7 +71,8 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         return os.path.join(BUILD, name + ".o")
 
     cu = [("boids_kernels.cu", ["boids_engine.h", "boids_softfp.h"]),
-          ("boids_noalloc.cu", ["boids_engine.h"])]
+          ("boids_noalloc.cu", ["boids_engine.h"]),
+          ("boids_mlp.cu", [])]
     for src, deps in cu:
         o = obj(os.path.splitext(src)[0])
         srcs = _sources(src, *deps) + HEADERS
@@ -93,7 +94,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for r in ex.map(_run, jobs):
             out.append(r)
-    objs = [obj("boids_kernels"), obj("boids_noalloc"), obj("boids_capi"), obj("boids_ensemble")]
+    objs = [obj("boids_kernels"), obj("boids_noalloc"), obj("boids_mlp"), obj("boids_capi"), obj("boids_ensemble")]
     if force or jobs or not os.path.exists(LIB):
         tmp = LIB + ".tmp%d" % os.getpid()
         _run(["g++", "-shared", "-o", tmp, *objs, "-L" + os.path.join(cuda, "lib64"),

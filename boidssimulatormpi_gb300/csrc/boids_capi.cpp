@@ -165,7 +165,7 @@ void free_buffers(DevBuffers &b)
 {
     void *ptrs[] = {b.pos[0], b.pos[1], b.vel[0], b.vel[1], b.key, b.rank, b.count, b.lstart,
                     b.bsum, b.ticket, b.ap_cnt, b.ap_list, b.forces, b.stage, b.cells8, b.dcnt, b.dhash,
-                    b.dense_list, b.dense_n, b.flag};
+                    b.dense_list, b.dense_n, b.flag, b.dflag, b.carry};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     b = DevBuffers{};
@@ -393,6 +393,7 @@ int make_constants(const boids_params &p, StepConst &k, bool *ref_ok)
     k.side = G ? (float)(p.field_size / G) : 0.f;
     k.trim_r2 = k.filt_r2 * 1.002f;
     k.dense_min = boidsgpu::kDenseMin;
+    k.lone_cand = boidsgpu::kLoneCand;
     k.defer_min = boidsgpu::kDeferMin;
     k.cand_defer = boidsgpu::kCandDefer;
     return BOIDS_OK;
@@ -450,11 +451,16 @@ int boids_create(const boids_params *params, boids_sim **out)
         ALLOC(&b.ticket, 1, true);
         const size_t ndense = boidsgpu::dense_list_capacity(b.ncell, n);
         ALLOC(&b.dense_list, ndense);
+        ALLOC(&b.dflag, b.ncell / 4);
+        {
+            unsigned char *carry = nullptr;
+            ALLOC(&carry, (size_t)boidsgpu::kCarryBytes * n);
+            b.carry = carry;
+        }
         ALLOC(&b.dense_n, 2, true);
         int nsm = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p.device);
         b.dense_grid = (uint32_t)std::max(1, nsm) * 4;
-        b.dense_min = k.dense_min;
     } else {
         b.ap_cap = boidsgpu::kApCap;
         ALLOC(&b.ap_cnt, n, true);
@@ -561,7 +567,7 @@ int boids_step(boids_sim *s, int32_t steps)
         if (s->engine == 1) {
             {
                 PhaseTimer pt(s, 0);
-                CK(boidsgpu::launch_grid_scan(s->b, s->stream, &s->launches));
+                CK(boidsgpu::launch_grid_scan(s->k, s->b, s->stream, &s->launches));
                 CK(boidsgpu::launch_grid_scatter(s->k, s->b, s->cur, true, s->stream, &s->launches));
                 s->acc.bin_launches += 2;
             }
@@ -608,6 +614,26 @@ int boids_get_forces(boids_sim *s, float *force9n)
     if (rc) return rc;
     CK(cudaMemcpyAsync(force9n, s->b.forces, sizeof(float) * 9 * s->k.n, cudaMemcpyDeviceToHost, s->stream));
     return boids_synchronize(s);
+}
+
+int boids_set_tuning(boids_sim *s, const int32_t *t)
+{
+    if (!s || !t) return fail(BOIDS_EINVAL, "boids_set_tuning: null argument");
+    for (int i = 0; i < 4; ++i)
+        if (t[i] < 0) return fail(BOIDS_EINVAL, "boids_set_tuning: negative threshold");
+    s->k.dense_min = (uint32_t)t[0];
+    s->k.defer_min = (uint32_t)t[1];
+    s->k.cand_defer = (uint32_t)t[2];
+    s->k.lone_cand = (uint32_t)t[3];
+    return BOIDS_OK;
+}
+
+int boids_get_tuning(boids_sim *s, int32_t *t)
+{
+    if (!s || !t) return fail(BOIDS_EINVAL, "boids_get_tuning: null argument");
+    const uint32_t v[4] = {s->k.dense_min, s->k.defer_min, s->k.cand_defer, s->k.lone_cand};
+    for (int i = 0; i < 4; ++i) t[i] = (int32_t)std::min<uint32_t>(v[i], 0x7fffffffu);
+    return BOIDS_OK;
 }
 
 int boids_frame_async(boids_sim *s, float *pframe, float *vframe, int32_t with_forces, int32_t slot)
@@ -685,7 +711,7 @@ int boids_get_neighbor_sets(boids_sim *s, int32_t *count3n, uint64_t *hash3n)
     if (!s->b.dcnt && (rc = dalloc(&s->b.dcnt, 3 * n))) return rc;
     if (!s->b.dhash && (rc = dalloc(&s->b.dhash, 3 * n))) return rc;
     if (s->engine == 1) {
-        CK(boidsgpu::launch_grid_scan(s->b, s->stream, &s->launches));
+        CK(boidsgpu::launch_grid_scan(s->k, s->b, s->stream, &s->launches));
         CK(boidsgpu::launch_grid_scatter(s->k, s->b, s->cur, false, s->stream, &s->launches));
         CK(boidsgpu::launch_grid_force(s->k, s->b, 1 - s->cur, true, false, s->stream, &s->launches));
     } else {

@@ -64,11 +64,10 @@ struct StepConst {
     uint32_t slot_off;
     uint32_t flock;
     // Which full-size cells the CTA-per-cell kernel takes (the results do not
-    // depend on it): those holding dense_min boids or more, and those holding
+    // depend on it): those holding dense_min boids or more, those holding
     // defer_min or more whose 27-cell neighbourhood holds over cand_defer
-    // boids.  kDeferMin <= defer_min <= dense_min.
-    uint32_t dense_min, defer_min, cand_defer;
-    uint32_t pad2;
+    // boids, and any non-empty cell whose neighbourhood holds over lone_cand.
+    uint32_t dense_min, defer_min, cand_defer, lone_cand;
 };
 
 // A batched ensemble's flock table, in device memory.  Every block of
@@ -99,27 +98,28 @@ struct DevBuffers {
     uint64_t *dhash;           // 3 per boid (id order)
     uint32_t *dense_list;      // full-size cells for the dense kernel, this step (dense_list_capacity)
     uint32_t *dense_n;         // their number, then the dense kernel's work queue (2 words)
+    uint8_t *dflag;            // per full-size cell: 1 when the dense kernel takes it
+    void *carry;               // per slot, kCarryBytes: partial sums between id windows (null: no windows)
     uint32_t *flag;            // set_state range check (1 word)
     uint32_t ncell, ncell_pad, nscan_blocks;
     uint32_t dense_grid;       // CTAs of the dense-cell kernel
-    uint32_t dense_min;        // the scan's listing threshold (= StepConst::dense_min)
     uint32_t ap_cap;
 };
 
 constexpr int kScanTile = 2048;       // cells per scan block (256 threads x 8)
 constexpr int kListCap = 32;          // grid engine, sparse cells: sorted neighbours kept per pass
 constexpr int kDenseMin = 12;         // default dense_min
-constexpr int kDeferMin = 4;          // smallest legal defer_min (and dense_min)
+constexpr int kDeferMin = 4;          // default defer_min
 constexpr int kCandDefer = 192;       // default cand_defer
+constexpr int kLoneCand = 384;        // default lone_cand
+constexpr int kCarryBytes = 72;       // partial sums of one boid between id windows
 
-// Entries the dense-cell work list can need in one step: a full-size cell
-// (4 x cells) is listed at most once, by the scan when it holds dense_min
-// boids or by its first boid when it holds defer_min or more, both at least
-// kDeferMin.
+// Entries the dense-cell work list can need in one step: each non-empty
+// full-size cell (4 x cells) is listed at most once.
 inline size_t dense_list_capacity(size_t ncell, size_t n)
 {
-    const size_t by_cells = ncell / 4, by_boids = n / kDeferMin;
-    return (by_cells < by_boids ? by_cells : by_boids) + 1;
+    const size_t by_cells = ncell / 4;
+    return (by_cells < n ? by_cells : n) + 1;
 }
 constexpr int kDenseCap = 2048;       // candidates of a dense cell held in shared memory
 constexpr int kApCap = 64;            // all-pairs engine: neighbours kept per boid
@@ -140,7 +140,10 @@ cudaError_t launch_frame(const float4 *pos4, const float4 *vel4, const float *fo
 cudaError_t launch_grid_keys(const StepConst &k, const float4 *pos, uint32_t *key, uint32_t *rank,
                              uint32_t *count, cudaStream_t s, uint64_t *launches,
                              const FlockTable *ft = nullptr);
-cudaError_t launch_grid_scan(const DevBuffers &b, cudaStream_t s, uint64_t *launches);
+// Scan of the cell counts, then the dense-cell classification (flags and
+// work list) of every full-size cell.
+cudaError_t launch_grid_scan(const StepConst &k, const DevBuffers &b, cudaStream_t s, uint64_t *launches,
+                             const FlockTable *ft = nullptr);
 cudaError_t launch_grid_scatter(const StepConst &k, const DevBuffers &b, int from, bool zero_counts,
                                 cudaStream_t s, uint64_t *launches, const FlockTable *ft = nullptr);
 // Rules + integration over the sorted state b.pos[from]; writes the new state

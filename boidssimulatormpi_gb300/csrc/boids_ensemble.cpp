@@ -50,9 +50,11 @@ int cuda_fail(cudaError_t e, const char *where)
 constexpr int kGraphSteps = 16;  // steps per captured graph
 
 // Dense-cell threshold candidates tried by the autotuner:
-// {dense_min, defer_min, cand_defer}; the first is the default.
-constexpr uint32_t kTuneCand[][3] = {
-    {12, 4, 192}, {8, 4, 128}, {16, 4, 256}, {24, 6, 384}, {6, 4, 96}, {12, 12, 1u << 30}, {1u << 30, 1u << 30, 0},
+// {dense_min, defer_min, cand_defer, lone_cand}; the first is the default.
+constexpr uint32_t kNever = 1u << 30;
+constexpr uint32_t kTuneCand[][4] = {
+    {12, 4, 192, 384}, {8, 4, 128, 256}, {16, 4, 256, 512}, {24, 6, 384, 768}, {6, 3, 96, 192},
+    {12, 4, 192, 2048}, {kNever, kNever, kNever, 1024},
 };
 
 }  // namespace
@@ -78,7 +80,7 @@ struct boids_ensemble {
     bool has_state = false;
     cudaGraphExec_t graph = nullptr;
     uint64_t launches = 0;
-    uint32_t tune[3] = {boidsgpu::kDenseMin, boidsgpu::kDeferMin, boidsgpu::kCandDefer};
+    uint32_t tune[4] = {boidsgpu::kDenseMin, boidsgpu::kDeferMin, boidsgpu::kCandDefer, boidsgpu::kLoneCand};
 };
 
 namespace {
@@ -88,7 +90,7 @@ void release(boids_ensemble *e)
     if (e->graph) cudaGraphExecDestroy(e->graph);
     DevBuffers &b = e->b;
     void *ptrs[] = {b.pos[0], b.pos[1], b.vel[0], b.vel[1], b.key, b.rank, b.count, b.lstart, b.bsum, b.ticket,
-                    b.dense_list, b.dense_n, e->d_ks, e->d_blk, e->d_cell4, e->d_link, e->d_acc, e->d_com,
+                    b.dense_list, b.dense_n, b.dflag, b.carry, e->d_ks, e->d_blk, e->d_cell4, e->d_link, e->d_acc, e->d_com,
                     e->d_largest, e->d_err};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -129,7 +131,7 @@ int bin_fresh(boids_ensemble *e)
 int step_once(boids_ensemble *e)
 {
     if (!e->binned) {
-        CK(boidsgpu::launch_grid_scan(e->b, e->stream, &e->launches));
+        CK(boidsgpu::launch_grid_scan(e->ks[0], e->b, e->stream, &e->launches, &e->ft));
         CK(boidsgpu::launch_grid_scatter(e->ks[0], e->b, e->cur, true, e->stream, &e->launches, &e->ft));
         e->cur = 1 - e->cur;
     }
@@ -143,7 +145,7 @@ int step_once(boids_ensemble *e)
 int bin_now(boids_ensemble *e)
 {
     if (e->binned) return 0;
-    CK(boidsgpu::launch_grid_scan(e->b, e->stream, &e->launches));
+    CK(boidsgpu::launch_grid_scan(e->ks[0], e->b, e->stream, &e->launches, &e->ft));
     CK(boidsgpu::launch_grid_scatter(e->ks[0], e->b, e->cur, true, e->stream, &e->launches, &e->ft));
     e->cur = 1 - e->cur;
     e->binned = true;
@@ -191,10 +193,10 @@ int upload_table(boids_ensemble *e)
         k.dense_min = e->tune[0];
         k.defer_min = e->tune[1];
         k.cand_defer = e->tune[2];
+        k.lone_cand = e->tune[3];
     }
-    e->b.dense_min = e->tune[0];
     CK(cudaMemcpyAsync(e->d_ks, e->ks.data(), sizeof(StepConst) * e->ks.size(), cudaMemcpyHostToDevice, e->stream));
-    if (e->graph) {  // the scan's threshold is a captured kernel argument
+    if (e->graph) {  // re-captured on the next step
         cudaGraphExecDestroy(e->graph);
         e->graph = nullptr;
     }
@@ -271,6 +273,12 @@ int boids_ensemble_create(const boids_flock_desc *flocks, uint32_t count, boids_
     ALLOC(&b.ticket, 1);
     ALLOC(&b.dense_list, boidsgpu::dense_list_capacity(b.ncell, e->total_boids));
     ALLOC(&b.dense_n, 2);
+    ALLOC(&b.dflag, b.ncell / 4);
+    {
+        unsigned char *carry = nullptr;
+        ALLOC(&carry, (size_t)boidsgpu::kCarryBytes * ns);
+        b.carry = carry;
+    }
     ALLOC(&e->d_ks, count);
     ALLOC(&e->d_blk, e->blk_flock.size());
     ALLOC(&e->d_cell4, count);
@@ -492,7 +500,8 @@ int boids_ensemble_autotune(boids_ensemble *e, int32_t steps_per_trial)
         cudaMemcpyAsync(sv, e->b.vel[0], bytes, cudaMemcpyDeviceToDevice, e->stream) != cudaSuccess ||
         cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess)
         rc = cuda_fail(cudaGetLastError(), "boids_ensemble_autotune");
-    const uint32_t keep[3] = {e->tune[0], e->tune[1], e->tune[2]};
+    uint32_t keep[4];
+    std::memcpy(keep, e->tune, sizeof keep);
     for (size_t c = 0; !rc && c < sizeof(kTuneCand) / sizeof(kTuneCand[0]); ++c) {
         std::memcpy(e->tune, kTuneCand[c], sizeof e->tune);
         if ((rc = upload_table(e)) || (rc = restore()) || (rc = step_once(e))) break;  // one warm-up step
@@ -522,10 +531,10 @@ int boids_ensemble_autotune(boids_ensemble *e, int32_t steps_per_trial)
     return rc ? rc : rc2;
 }
 
-int boids_ensemble_tuning(boids_ensemble *e, int32_t *out3)
+int boids_ensemble_tuning(boids_ensemble *e, int32_t *out4)
 {
-    if (!e || !out3) return fail(BOIDS_EINVAL, "boids_ensemble_tuning: bad argument");
-    for (int i = 0; i < 3; ++i) out3[i] = (int32_t)std::min<uint32_t>(e->tune[i], 0x7fffffffu);
+    if (!e || !out4) return fail(BOIDS_EINVAL, "boids_ensemble_tuning: bad argument");
+    for (int i = 0; i < 4; ++i) out4[i] = (int32_t)std::min<uint32_t>(e->tune[i], 0x7fffffffu);
     return BOIDS_OK;
 }
 

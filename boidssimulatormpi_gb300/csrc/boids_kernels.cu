@@ -127,6 +127,7 @@ struct Acc {
     int ncoh, nsep, nali;
     uint64_t h[3];
 };
+static_assert(sizeof(Acc) == kCarryBytes, "the carry buffer holds one Acc per slot");
 
 __device__ __forceinline__ void acc_zero(Acc &a)
 {
@@ -300,6 +301,7 @@ struct GridOut {
     float *forces;
     int32_t *dcnt;
     uint64_t *dhash;
+    Acc *carry;  // per slot: partial sums of huge cells between id windows (null: no windows)
 };
 
 template <bool DIAG>
@@ -407,8 +409,7 @@ __global__ void k_grid_keys(const float4 *__restrict__ pos, uint32_t *__restrict
 // Exclusive scan of the per-cell counts.  Each block scans one tile of
 // kScanTile cells into lstart and publishes its total; the last block to
 // finish (completion ticket, no waiting) turns the totals into tile offsets
-// in bsum.  start(c) = lstart[c] + bsum[c / kScanTile].  Cells holding at
-// least dense_min boids are appended to the dense-cell work list.
+// in bsum.  start(c) = lstart[c] + bsum[c / kScanTile].
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = kScanTile / kScanThreads;  // 8
 
@@ -442,8 +443,7 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *warp_t
 
 __global__ void __launch_bounds__(kScanThreads)
 k_grid_scan(const uint32_t *__restrict__ count, uint32_t *__restrict__ lstart, uint32_t *bsum,
-            uint32_t *ticket, uint32_t nblocks, uint32_t *__restrict__ dense_list, uint32_t *dense_n,
-            uint32_t dense_min)
+            uint32_t *ticket, uint32_t nblocks)
 {
     __shared__ uint32_t warp_tot[kScanThreads / 32];
     __shared__ bool is_last;
@@ -454,10 +454,6 @@ k_grid_scan(const uint32_t *__restrict__ count, uint32_t *__restrict__ lstart, u
     uint32_t sum = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) sum += v[i];
-    if (dense_list) {  // a full-size cell is 4 consecutive x cells; base is a multiple of 8
-        if (v[0] + v[1] + v[2] + v[3] >= dense_min) dense_list[atomicAdd(dense_n, 1u)] = base / 4;
-        if (v[4] + v[5] + v[6] + v[7] >= dense_min) dense_list[atomicAdd(dense_n, 1u)] = base / 4 + 1;
-    }
     uint32_t total;
     uint32_t run = block_excl_scan<kScanThreads>(sum, warp_tot, total);
     uint32_t o[8];
@@ -540,13 +536,57 @@ __device__ __forceinline__ Seg segment(int cx, int cy, int cz, int q, int runs, 
     return run == 0 ? Seg{r0 + Gx - 8, r0 + Gx, 0.f, sy, sz} : Seg{r0, r0 + 4, k.Ff, sy, sz};
 }
 
-// Which kernel takes the boids of a cell: k_grid_dense when its shared
-// candidate list fits and either the cell is crowded or it holds a few boids
-// and its neighbourhood is crowded (then sorting once per cell beats sorting
-// per boid), else k_grid_sparse.
-__device__ __forceinline__ bool dense_path(uint32_t b, uint32_t ncand, const StepConst &k)
+// Which kernel takes the boids of a full-size cell: k_grid_dense when the
+// cell is crowded (dense_min boids or more), or holds defer_min or more with
+// over cand_defer candidates in its 27 cells, or holds any boid with over
+// lone_cand candidates (sorting a crowded neighbourhood once per cell beats
+// sorting it per boid); else k_grid_sparse.  Cells with more than kDenseCap
+// candidates need the dense kernel's id windows (windows != 0).
+__device__ __forceinline__ bool dense_rule(uint32_t b, uint32_t ncand, const StepConst &k, int windows)
 {
-    return ncand <= (uint32_t)kDenseCap && (b >= k.dense_min || (b >= k.defer_min && ncand > k.cand_defer));
+    const bool want = b >= k.dense_min || (b >= k.defer_min && ncand > k.cand_defer) || ncand > k.lone_cand;
+    return b > 0 && want && (ncand <= (uint32_t)kDenseCap || windows);
+}
+
+// Per full-size cell, after the scan and before the scatter (the counts are
+// still intact): the dense flag the thread-per-boid kernel reads, and the
+// dense kernel's work list.
+template <bool MULTI>
+__global__ void k_grid_classify(const uint32_t *__restrict__ count, const uint32_t *__restrict__ lstart,
+                                const uint32_t *__restrict__ bsum, uint8_t *__restrict__ dflag,
+                                uint32_t *__restrict__ dense_list, uint32_t *__restrict__ dense_n, uint32_t nfull,
+                                int windows, StepConst kp, FlockTable ft)
+{
+    const uint32_t cg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cg >= nfull) return;
+    const uint4 c4 = *reinterpret_cast<const uint4 *>(count + 4 * (size_t)cg);
+    const uint32_t b = c4.x + c4.y + c4.z + c4.w;
+    uint8_t flag = 0;
+    if (b > 0) {
+        uint32_t f = 0;
+        if (MULTI) {  // the flock: last with cell4 <= cg
+            uint32_t hi = ft.count;
+            while (hi - f > 1) {
+                const uint32_t mid = (f + hi) / 2;
+                if (__ldg(ft.cell4 + mid) <= cg) f = mid; else hi = mid;
+            }
+        }
+        const StepConst &k = MULTI ? ft.ks[f] : kp;
+        const uint32_t c = cg - k.cell_base / 4;
+        const int G = k.G;
+        const int cx = (int)(c % G), cy = (int)((c / G) % G), cz = (int)(c / ((uint32_t)G * G));
+        const int runs = seg_runs(cx, k);
+        uint32_t ncand = 0;
+        for (int q = 0; q < 9 * runs; ++q) {
+            const Seg sg = segment(cx, cy, cz, q, runs, k);
+            ncand += cell_start(lstart, bsum, k.cell_base + sg.c1) - cell_start(lstart, bsum, k.cell_base + sg.c0);
+        }
+        if (dense_rule(b, ncand, k, windows)) {
+            flag = 1;
+            dense_list[atomicAdd(dense_n, 1u)] = cg;
+        }
+    }
+    dflag[cg] = flag;
 }
 
 // ------------------------------------------------------------------ sparse cells: thread per boid
@@ -574,6 +614,7 @@ struct GridIn {
     const float4 *__restrict__ vel;
     const uint32_t *__restrict__ lstart;
     const uint32_t *__restrict__ bsum;
+    const uint8_t *__restrict__ dflag;  // per full-size cell: taken by k_grid_dense
 };
 
 struct SparseSmem {
@@ -585,8 +626,7 @@ struct SparseSmem {
 
 template <bool DIAG, bool MULTI>
 __global__ void __launch_bounds__(kRT)
-k_grid_sparse(GridIn g, GridOut o, uint32_t *__restrict__ dense_list, uint32_t *__restrict__ dense_n, StepConst kp,
-              FlockTable ft)
+k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
 {
     static_assert(kRT == kSlotAlign, "a CTA serves one flock");
     __shared__ SparseSmem sm;
@@ -608,29 +648,8 @@ k_grid_sparse(GridIn g, GridOut o, uint32_t *__restrict__ dense_list, uint32_t *
         yy = yy < 0 ? yy + G : (yy >= G ? yy - G : yy);
         return k.cell_base + (uint32_t)(zz * G + yy) * (uint32_t)Gx;
     };
-    if (act) {
-        const uint32_t x0 = 4 * (uint32_t)cx, own_row = row_base(4);
-        const uint32_t own0 = slot_start(g.lstart, g.bsum, own_row + x0, k);
-        const uint32_t b = slot_start(g.lstart, g.bsum, own_row + x0 + 4, k) - own0;
-        if (b >= k.defer_min) {
-            // Which kernel: the count of the 27 full-size cells around the
-            // boid's cell, exactly as k_grid_dense computes it.
-            uint32_t ncell27 = 0;
-            const int runs = seg_runs(cx, k);
-            for (int q = 0; q < 9 * runs; ++q) {
-                const Seg sg = segment(cx, cy, cz, q, runs, k);
-                ncell27 += cell_start(g.lstart, g.bsum, k.cell_base + sg.c1) -
-                           cell_start(g.lstart, g.bsum, k.cell_base + sg.c0);
-            }
-            if (dense_path(b, ncell27, k)) {
-                // a crowded cell is listed by the scan; a cell with a crowded
-                // neighbourhood is listed here, once, by its first boid
-                if (b < k.dense_min && s == own0)
-                    dense_list[atomicAdd(dense_n, 1u)] = own_row / 4 + (uint32_t)cx;
-                act = false;
-            }
-        }
-    }
+    // boids of dense cells are k_grid_dense's
+    if (act && __ldg(g.dflag + row_base(4) / 4 + (uint32_t)cx)) act = false;
     // This boid's segments: in each neighbour row, the x cells that a sphere
     // of radius sqrt(trim_r2) around it reaches.
     int nseg = 0;
@@ -813,6 +832,8 @@ struct DenseSmem {
     uint32_t seg_j0[18], seg_k0[19];
     float seg_s[18][3];
     uint32_t work, flock;
+    uint32_t nw, cut;              // huge cells: window size, histogram cut
+    uint32_t wtot[kDT / 32];       // block scan scratch
     StepConst kf;  // the current cell's flock (batched ensembles)
 };
 static_assert(kDenseCap <= 2048, "gather index must fit 11 bits");
@@ -836,6 +857,68 @@ __device__ __forceinline__ float3 cand_image(float4 c, float3 pi, const float4 *
 // over in id order and the owner folds them in after its own, so the
 // accumulation order stays ascending id.  A chunk lane whose hand-over list
 // overflows leaves its chunk to the owner.
+// Id window of a huge cell (more than kDenseCap candidates): the largest hi
+// such that the candidates with ids in [lo, hi) fit the shared list.  A
+// histogram of the candidates' ids over kWinBins bins is cut where the
+// running count passes kDenseCap; if the first bin alone is over, the span
+// narrows to that bin.  A boid is a candidate at most once (G >= 3), so a
+// bin one id wide always fits and the search ends.
+constexpr int kWinBins = 4096;
+
+__device__ uint32_t dense_window(DenseSmem &sm, const GridIn &g, int ns, uint32_t lo, uint32_t nid)
+{
+    static_assert(kWinBins * 4 <= sizeof(sm.u.keys[0]), "window histogram lives in the first sort buffer");
+    static_assert(kWinBins % kDT == 0, "bins per thread");
+    constexpr int kPer = kWinBins / kDT;
+    uint32_t *hist = reinterpret_cast<uint32_t *>(sm.u.keys[0]);
+    const int t = threadIdx.x;
+    uint32_t span_hi = nid;
+    for (;;) {
+        const uint32_t w = (span_hi - lo + kWinBins - 1) / kWinBins;
+        for (int i = t; i < kWinBins; i += kDT) hist[i] = 0;
+        if (t == 0) sm.cut = kWinBins;
+        __syncthreads();
+        for (int sgi = 0; sgi < ns; ++sgi) {
+            const uint32_t j0 = sm.seg_j0[sgi], len = sm.seg_k0[sgi + 1] - sm.seg_k0[sgi];
+            for (uint32_t q = t; q < len; q += kDT) {
+                const uint32_t id = __float_as_uint(__ldg(&g.pos[j0 + q].w));
+                if (id >= lo && id < span_hi) atomicAdd(&hist[(id - lo) / w], 1u);
+            }
+        }
+        __syncthreads();
+        uint32_t loc = 0;
+#pragma unroll 8
+        for (int i = 0; i < kPer; ++i) loc += hist[t * kPer + i];
+        uint32_t total;
+        uint32_t run = block_excl_scan<kDT>(loc, sm.wtot, total);
+        if (run + loc > (uint32_t)kDenseCap) {
+            for (int i = 0; i < kPer; ++i) {
+                run += hist[t * kPer + i];
+                if (run > (uint32_t)kDenseCap) {
+                    atomicMin(&sm.cut, (uint32_t)(t * kPer + i));
+                    break;
+                }
+            }
+        }
+        __syncthreads();
+        const uint32_t cut = sm.cut;
+        __syncthreads();  // hist and cut are rewritten next
+        if (cut >= (uint32_t)kWinBins) return span_hi;
+        if (cut > 0) return lo + cut * w;
+        span_hi = lo + w;  // w > 1 here: a one-id bin holds at most one candidate
+    }
+}
+
+// One CTA takes one crowded cell at a time (dynamic queue).  The cell's
+// 27-cell candidates are radix-sorted by id once.  The cell's b boids x the
+// candidate list is then split over all threads: each boid gets L = 128/b
+// lanes, lane l walks chunk l of the id-ordered list; chunk 0's lane (the
+// owner) accumulates its accepted neighbours at once, the others hand theirs
+// over in id order and the owner folds them in after its own, so the
+// accumulation order stays ascending id.  A chunk lane whose hand-over list
+// overflows leaves its chunk to the owner.  A cell with more than kDenseCap
+// candidates is done in ascending id windows that each fit the list; the
+// owners carry their partial sums from window to window through o.carry.
 template <bool DIAG, bool MULTI>
 __global__ void __launch_bounds__(kDT, 4)
 k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint32_t *__restrict__ dense_n,
@@ -882,132 +965,163 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
         const uint32_t ncand = sm.seg_k0[ns];
         const uint32_t own0 = slot_start(g.lstart, g.bsum, 4 * cg, k);
         const uint32_t b = slot_start(g.lstart, g.bsum, 4 * cg + 4, k) - own0;
-        if (!dense_path(b, ncand, k)) {  // too many candidates: left to k_grid_sparse
+        const bool huge = ncand > (uint32_t)kDenseCap;
+        if (huge && !o.carry) {  // not listed so by k_grid_classify; kept for safety
             __syncthreads();
             continue;
         }
 
-        // gather (id, segment, gather index) keys and sort them by id
-        for (uint32_t q = t; q < ncand; q += kDT) {
-            uint32_t sgi = 0;
-            while (q >= sm.seg_k0[sgi + 1]) ++sgi;
-            const uint32_t slot = sm.seg_j0[sgi] + (q - sm.seg_k0[sgi]);
-            sm.v.s.gslot[q] = slot;
-            sm.u.keys[0][q] = ((uint64_t)__float_as_uint(__ldg(&g.pos[slot].w)) << 16) | (sgi << 11) | q;
-        }
-        __syncthreads();
-        const uint64_t *sorted =
-            block_radix_sort<kDT>(sm.u.keys[0], sm.u.keys[1], sm.v.s.hist, (int)ncand, 16, k.id_bits);
-        // lay the candidates out in id order over the dead sort buffers
-        const int K = ((int)ncand + kDT - 1) / kDT;
-        const int q0 = t * K;
-        uint32_t slot_r[kDenseKT], seg_r[kDenseKT];
-#pragma unroll
-        for (int i = 0; i < kDenseKT; ++i) {
-            if (i < K && q0 + i < (int)ncand) {
-                const uint64_t key = sorted[q0 + i];
-                slot_r[i] = sm.v.s.gslot[(uint32_t)key & 0x7ffu];
-                seg_r[i] = ((uint32_t)key >> 11) & 0x1fu;
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int i = 0; i < kDenseKT; ++i) {
-            if (i < K && q0 + i < (int)ncand) {
-                const float4 p = __ldg(g.pos + slot_r[i]);
-                const float *sh = sm.seg_s[seg_r[i]];
-                const bool wrapped = sh[0] != 0.f || sh[1] != 0.f || sh[2] != 0.f;
-                sm.u.spos[q0 + i] = wrapped ? make_float4(p.x + sh[0], p.y + sh[1], p.z + sh[2],
-                                                          __uint_as_float(slot_r[i] | 0x80000000u))
-                                            : make_float4(p.x, p.y, p.z, __uint_as_float(slot_r[i]));
-            }
-        }
-        __syncthreads();
-
-        for (uint32_t r0 = 0; r0 < b; r0 += kDT) {
-            const uint32_t nbr = min(b - r0, (uint32_t)kDT);      // boids this round
-            const uint32_t L = (uint32_t)kDT / nbr;               // lanes per boid
-            const uint32_t csz = (ncand + L - 1) / L;             // chunk length
-            const bool act = (uint32_t)t < nbr * L;
-            const uint32_t bi = act ? (uint32_t)t % nbr : 0, l = act ? (uint32_t)t / nbr : 0;
-            const uint32_t k0 = act ? min(ncand, l * csz) : 0, k1 = act ? min(ncand, k0 + csz) : 0;
-            const uint32_t s = own0 + r0 + bi;
-            const float4 p4 = g.pos[s], v4 = g.vel[s];
-            const float3 pi = xyz(p4), vi = xyz(v4);
-            const Sight sight = make_sight(vi);
-            Acc a;
-            acc_zero(a);
-            int nb = 0, nl = 0;
-            bool ovf = false;
-            const uint32_t len = k1 - k0;
-            const uint32_t maxlen = __reduce_max_sync(0xffffffffu, len);
-            for (uint32_t it = 0; it < maxlen; ++it) {
-                if (it < len) {
-                    const uint32_t q = k0 + it;
-                    const float4 cq = sm.u.spos[q];
-                    const float dx = cq.x - pi.x, dy = cq.y - pi.y, dz = cq.z - pi.z;
-                    const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                    if (d2 < k.filt_r2) sm.bufs[nb++ * kDT + t] = (uint16_t)q;
-                }
-                // exact tests of the buffered hits, the whole warp together
-                if (__any_sync(0xffffffffu, nb == kBufB) || it + 1 == maxlen) {
-                    for (int e = 0; e < nb; ++e) {
-                        const uint32_t q = sm.bufs[e * kDT + t];
-                        const float4 cq = sm.u.spos[q];
-                        const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
-                        if (j == s) continue;
-                        const float3 tt = cand_image(cq, pi, g.pos, k);
-                        const int f = pair_flags(pi, sight, tt, k);
-                        if (!f) continue;
-                        if (l == 0) {
-                            const float3 vj = (f & 4) ? xyz(__ldg(g.vel + j)) : make_float3(0.f, 0.f, 0.f);
-                            acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
-                        } else if (nl < kChunkList) {
-                            sm.v.lists[t * kChunkList + nl++] = q | ((uint32_t)f << 16);
-                        } else {
-                            ovf = true;
+        uint32_t lo = 0;  // this window's ids: [lo, hi)
+        for (;;) {
+            uint32_t hi = k.n, nw = ncand;
+            if (huge) {
+                hi = dense_window(sm, g, ns, lo, k.n);
+                // gather the window's (id, segment, gather index) keys
+                if (t == 0) sm.nw = 0;
+                __syncthreads();
+                for (int sgi = 0; sgi < ns; ++sgi) {
+                    const uint32_t j0 = sm.seg_j0[sgi], len = sm.seg_k0[sgi + 1] - sm.seg_k0[sgi];
+                    for (uint32_t q = t; q < len; q += kDT) {
+                        const uint32_t slot = j0 + q;
+                        const uint32_t id = __float_as_uint(__ldg(&g.pos[slot].w));
+                        if (id >= lo && id < hi) {
+                            const uint32_t qq = atomicAdd(&sm.nw, 1u);
+                            sm.v.s.gslot[qq] = slot;
+                            sm.u.keys[0][qq] = ((uint64_t)id << 16) | ((uint32_t)sgi << 11) | qq;
                         }
                     }
-                    nb = 0;
+                }
+                __syncthreads();
+                nw = sm.nw;
+            } else {
+                // gather every candidate's (id, segment, gather index) key
+                for (uint32_t q = t; q < ncand; q += kDT) {
+                    uint32_t sgi = 0;
+                    while (q >= sm.seg_k0[sgi + 1]) ++sgi;
+                    const uint32_t slot = sm.seg_j0[sgi] + (q - sm.seg_k0[sgi]);
+                    sm.v.s.gslot[q] = slot;
+                    sm.u.keys[0][q] = ((uint64_t)__float_as_uint(__ldg(&g.pos[slot].w)) << 16) | (sgi << 11) | q;
+                }
+                __syncthreads();
+            }
+            const uint64_t *sorted =
+                block_radix_sort<kDT>(sm.u.keys[0], sm.u.keys[1], sm.v.s.hist, (int)nw, 16, k.id_bits);
+            // lay the candidates out in id order over the dead sort buffers
+            const int K = ((int)nw + kDT - 1) / kDT;
+            const int q0 = t * K;
+            uint32_t slot_r[kDenseKT], seg_r[kDenseKT];
+#pragma unroll
+            for (int i = 0; i < kDenseKT; ++i) {
+                if (i < K && q0 + i < (int)nw) {
+                    const uint64_t key = sorted[q0 + i];
+                    slot_r[i] = sm.v.s.gslot[(uint32_t)key & 0x7ffu];
+                    seg_r[i] = ((uint32_t)key >> 11) & 0x1fu;
                 }
             }
-            sm.nlist[t] = (uint16_t)nl;
-            sm.ovf[t] = ovf;
             __syncthreads();
-            if (act && l == 0) {
-                // fold the other chunks' neighbours in, in chunk (= id) order
-                for (uint32_t ll = 1; ll < L; ++ll) {
-                    const uint32_t tt_ = ll * nbr + bi;
-                    if (sm.ovf[tt_]) {
-                        const uint32_t c0 = min(ncand, ll * csz), c1 = min(ncand, c0 + csz);
-                        for (uint32_t q = c0; q < c1; ++q) {
+#pragma unroll
+            for (int i = 0; i < kDenseKT; ++i) {
+                if (i < K && q0 + i < (int)nw) {
+                    const float4 p = __ldg(g.pos + slot_r[i]);
+                    const float *sh = sm.seg_s[seg_r[i]];
+                    const bool wrapped = sh[0] != 0.f || sh[1] != 0.f || sh[2] != 0.f;
+                    sm.u.spos[q0 + i] = wrapped ? make_float4(p.x + sh[0], p.y + sh[1], p.z + sh[2],
+                                                              __uint_as_float(slot_r[i] | 0x80000000u))
+                                                : make_float4(p.x, p.y, p.z, __uint_as_float(slot_r[i]));
+                }
+            }
+            __syncthreads();
+            const bool first = lo == 0, last = hi >= k.n;
+
+            for (uint32_t r0 = 0; r0 < b; r0 += kDT) {
+                const uint32_t nbr = min(b - r0, (uint32_t)kDT);      // boids this round
+                const uint32_t L = (uint32_t)kDT / nbr;               // lanes per boid
+                const uint32_t csz = (nw + L - 1) / L;                // chunk length
+                const bool act = (uint32_t)t < nbr * L;
+                const uint32_t bi = act ? (uint32_t)t % nbr : 0, l = act ? (uint32_t)t / nbr : 0;
+                const uint32_t k0 = act ? min(nw, l * csz) : 0, k1 = act ? min(nw, k0 + csz) : 0;
+                const uint32_t s = own0 + r0 + bi;
+                const float4 p4 = g.pos[s], v4 = g.vel[s];
+                const float3 pi = xyz(p4), vi = xyz(v4);
+                const Sight sight = make_sight(vi);
+                Acc a;
+                if (act && l == 0 && !first) a = o.carry[s];  // the earlier windows' sums
+                else acc_zero(a);
+                int nb = 0, nl = 0;
+                bool ovf = false;
+                const uint32_t len = k1 - k0;
+                const uint32_t maxlen = __reduce_max_sync(0xffffffffu, len);
+                for (uint32_t it = 0; it < maxlen; ++it) {
+                    if (it < len) {
+                        const uint32_t q = k0 + it;
+                        const float4 cq = sm.u.spos[q];
+                        const float dx = cq.x - pi.x, dy = cq.y - pi.y, dz = cq.z - pi.z;
+                        const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                        if (d2 < k.filt_r2) sm.bufs[nb++ * kDT + t] = (uint16_t)q;
+                    }
+                    // exact tests of the buffered hits, the whole warp together
+                    if (__any_sync(0xffffffffu, nb == kBufB) || it + 1 == maxlen) {
+                        for (int e = 0; e < nb; ++e) {
+                            const uint32_t q = sm.bufs[e * kDT + t];
                             const float4 cq = sm.u.spos[q];
-                            const float dx = cq.x - pi.x, dy = cq.y - pi.y, dz = cq.z - pi.z;
-                            const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
                             const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
-                            if (!(d2 < k.filt_r2) || j == s) continue;
+                            if (j == s) continue;
                             const float3 tt = cand_image(cq, pi, g.pos, k);
                             const int f = pair_flags(pi, sight, tt, k);
                             if (!f) continue;
-                            const float3 vj = (f & 4) ? xyz(__ldg(g.vel + j)) : make_float3(0.f, 0.f, 0.f);
-                            acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
+                            if (l == 0) {
+                                const float3 vj = (f & 4) ? xyz(__ldg(g.vel + j)) : make_float3(0.f, 0.f, 0.f);
+                                acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
+                            } else if (nl < kChunkList) {
+                                sm.v.lists[t * kChunkList + nl++] = q | ((uint32_t)f << 16);
+                            } else {
+                                ovf = true;
+                            }
                         }
-                    } else {
-                        const uint32_t m = sm.nlist[tt_];
-                        for (uint32_t e = 0; e < m; ++e) {
-                            const uint32_t v = sm.v.lists[tt_ * kChunkList + e];
-                            const float4 cq = sm.u.spos[v & 0xffffu];
-                            const int f = (int)(v >> 16);
-                            const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
-                            const float3 tt = cand_image(cq, pi, g.pos, k);
-                            const float3 vj = (f & 4) ? xyz(__ldg(g.vel + j)) : make_float3(0.f, 0.f, 0.f);
-                            acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
-                        }
+                        nb = 0;
                     }
                 }
-                finish_boid<DIAG>(a, p4, vi, s, o, k);
+                sm.nlist[t] = (uint16_t)nl;
+                sm.ovf[t] = ovf;
+                __syncthreads();
+                if (act && l == 0) {
+                    // fold the other chunks' neighbours in, in chunk (= id) order
+                    for (uint32_t ll = 1; ll < L; ++ll) {
+                        const uint32_t tt_ = ll * nbr + bi;
+                        if (sm.ovf[tt_]) {
+                            const uint32_t c0 = min(nw, ll * csz), c1 = min(nw, c0 + csz);
+                            for (uint32_t q = c0; q < c1; ++q) {
+                                const float4 cq = sm.u.spos[q];
+                                const float dx = cq.x - pi.x, dy = cq.y - pi.y, dz = cq.z - pi.z;
+                                const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                                const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
+                                if (!(d2 < k.filt_r2) || j == s) continue;
+                                const float3 tt = cand_image(cq, pi, g.pos, k);
+                                const int f = pair_flags(pi, sight, tt, k);
+                                if (!f) continue;
+                                const float3 vj = (f & 4) ? xyz(__ldg(g.vel + j)) : make_float3(0.f, 0.f, 0.f);
+                                acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
+                            }
+                        } else {
+                            const uint32_t m = sm.nlist[tt_];
+                            for (uint32_t e = 0; e < m; ++e) {
+                                const uint32_t v = sm.v.lists[tt_ * kChunkList + e];
+                                const float4 cq = sm.u.spos[v & 0xffffu];
+                                const int f = (int)(v >> 16);
+                                const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
+                                const float3 tt = cand_image(cq, pi, g.pos, k);
+                                const float3 vj = (f & 4) ? xyz(__ldg(g.vel + j)) : make_float3(0.f, 0.f, 0.f);
+                                acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
+                            }
+                        }
+                    }
+                    if (last) finish_boid<DIAG>(a, p4, vi, s, o, k);
+                    else o.carry[s] = a;
+                }
+                __syncthreads();  // lists and buffers are reused by the next round
             }
-            __syncthreads();  // lists and buffers are reused by the next round
+            if (last) break;
+            lo = hi;
         }
     }
 }
@@ -1192,13 +1306,22 @@ cudaError_t launch_grid_keys(const StepConst &k, const float4 *pos, uint32_t *ke
     return cudaGetLastError();
 }
 
-cudaError_t launch_grid_scan(const DevBuffers &b, cudaStream_t st, uint64_t *launches)
+cudaError_t launch_grid_scan(const StepConst &k, const DevBuffers &b, cudaStream_t st, uint64_t *launches,
+                             const FlockTable *ft)
 {
     cudaError_t e = cudaMemsetAsync(b.dense_n, 0, 2 * sizeof(uint32_t), st);  // count, work queue
     if (e != cudaSuccess) return e;
-    k_grid_scan<<<b.nscan_blocks, kScanThreads, 0, st>>>(b.count, b.lstart, b.bsum, b.ticket, b.nscan_blocks,
-                                                          b.dense_list, b.dense_n, b.dense_min);
-    ++*launches;
+    k_grid_scan<<<b.nscan_blocks, kScanThreads, 0, st>>>(b.count, b.lstart, b.bsum, b.ticket, b.nscan_blocks);
+    const uint32_t nfull = b.ncell / 4;
+    const int windows = b.carry != nullptr;
+    if (ft)
+        k_grid_classify<true><<<blocks_for(nfull, 256), 256, 0, st>>>(b.count, b.lstart, b.bsum, b.dflag,
+                                                                       b.dense_list, b.dense_n, nfull, windows, k, *ft);
+    else
+        k_grid_classify<false><<<blocks_for(nfull, 256), 256, 0, st>>>(b.count, b.lstart, b.bsum, b.dflag,
+                                                                        b.dense_list, b.dense_n, nfull, windows, k,
+                                                                        FlockTable{});
+    *launches += 2;
     return cudaGetLastError();
 }
 
@@ -1244,7 +1367,7 @@ cudaError_t grid_force(const StepConst &k, const GridIn &g, const GridOut &o, co
 {
     cudaError_t e = dense_smem_opt_in<DIAG, MULTI>();
     if (e != cudaSuccess) return e;
-    k_grid_sparse<DIAG, MULTI><<<nsp, kRT, 0, st>>>(g, o, b.dense_list, b.dense_n, k, ft);
+    k_grid_sparse<DIAG, MULTI><<<nsp, kRT, 0, st>>>(g, o, k, ft);
     k_grid_dense<DIAG, MULTI><<<b.dense_grid, kDT, sizeof(DenseSmem), st>>>(g, o, b.dense_list, b.dense_n, k, ft);
     return cudaGetLastError();
 }
@@ -1256,8 +1379,9 @@ cudaError_t launch_grid_force(const StepConst &k, const DevBuffers &b, int from,
 {
     const uint32_t n = ft ? ft->nslots : k.n;
     if (n == 0) return cudaSuccess;
-    GridIn g{b.pos[from], b.vel[from], b.lstart, b.bsum};
+    GridIn g{b.pos[from], b.vel[from], b.lstart, b.bsum, b.dflag};
     GridOut o{};
+    o.carry = static_cast<Acc *>(b.carry);
     if (diag) {
         o.dcnt = b.dcnt;
         o.dhash = b.dhash;

@@ -1,0 +1,498 @@
+// boids_mlp.cu -- the sweep surrogate's network on the tensor cores.
+//
+// A multilayer perceptron in -> hidden -> hidden -> out with ReLU, BF16
+// weights and activations and FP32 accumulation, trained with Adam on the
+// mean squared error.  It maps a flock's rule parameters to its order
+// statistics after a run (the ensemble's boids_ensemble_stats), so that a
+// parameter sweep can be screened before the plain simulation re-runs the
+// candidates it selects.  No counterpart in the reference.
+//
+// Every product -- forward, the input gradient and the weight gradient of
+// the backward pass -- is one strided GEMM kernel on mma.sync m16n8k16
+// (BF16 operands, FP32 accumulators): the layer widths (8, 256, 4) make
+// these small, latency-bound products, where a warp-level MMA with operands
+// read straight from L2 is the simplest fast form.
+#include "boids.h"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace boidsgpu {
+int set_last_error(int code, const char *msg);
+}
+
+namespace {
+
+// A read-only BF16 matrix view: element (r, c) at p[r * rs + c * cs].
+struct MatB {
+    const __nv_bfloat16 *p;
+    long long rs, cs;
+    int rows, cols;
+};
+
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi)
+{
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+__device__ __forceinline__ __nv_bfloat16 at(const MatB &m, int r, int c)
+{
+    return (r < m.rows && c < m.cols) ? m.p[r * m.rs + c * m.cs] : __float2bfloat16_rn(0.f);
+}
+
+constexpr int kWarpsM = 4;   // warps per CTA along M (16 rows each)
+constexpr int kTileN = 32;   // columns per warp (4 MMA tiles of 8)
+
+// C = A (M x K) * B (K x N) [+ bias] [* (mask > 0)], FP32 out (row-major,
+// ldc) and optionally a BF16 copy of relu(C) or C (row-major, ldb16).
+__global__ void __launch_bounds__(32 * kWarpsM)
+k_mlp_gemm(MatB A, MatB B, float *__restrict__ C, int ldc, __nv_bfloat16 *__restrict__ C16, int ld16,
+           const float *__restrict__ bias, const float *__restrict__ mask, int ldm, int relu16)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, t4 = lane & 3;
+    const int r0 = (blockIdx.y * kWarpsM + warp) * 16;
+    const int n0 = blockIdx.x * kTileN;
+    const int M = A.rows, K = A.cols, N = B.cols;
+    if (r0 >= M) return;
+    float acc[4][4] = {};
+    for (int kk = 0; kk < K; kk += 16) {
+        const int ka = kk + 2 * t4;
+        uint32_t a[4];
+        a[0] = pack2(at(A, r0 + g, ka), at(A, r0 + g, ka + 1));
+        a[1] = pack2(at(A, r0 + g + 8, ka), at(A, r0 + g + 8, ka + 1));
+        a[2] = pack2(at(A, r0 + g, ka + 8), at(A, r0 + g, ka + 9));
+        a[3] = pack2(at(A, r0 + g + 8, ka + 8), at(A, r0 + g + 8, ka + 9));
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int n = n0 + 8 * j + g;
+            const uint32_t b0 = pack2(at(B, ka, n), at(B, ka + 1, n));
+            const uint32_t b1 = pack2(at(B, ka + 8, n), at(B, ka + 9, n));
+            asm volatile(
+                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+                "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};\n"
+                : "+f"(acc[j][0]), "+f"(acc[j][1]), "+f"(acc[j][2]), "+f"(acc[j][3])
+                : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int r = r0 + g + (q >= 2 ? 8 : 0);
+            const int c = n0 + 8 * j + 2 * t4 + (q & 1);
+            if (r >= M || c >= N) continue;
+            float v = acc[j][q];
+            if (bias) v += bias[c];
+            if (mask && !(mask[(long long)r * ldm + c] > 0.f)) v = 0.f;
+            if (C) C[(long long)r * ldc + c] = v;
+            if (C16) C16[(long long)r * ld16 + c] = __float2bfloat16_rn(relu16 ? fmaxf(v, 0.f) : v);
+        }
+    }
+}
+
+// Mean squared error over rows x cols and its gradient 2 (y - t) / (rows * cols).
+__global__ void k_mlp_mse(const float *__restrict__ y, const float *__restrict__ t, int n, float scale,
+                          float *__restrict__ dy, __nv_bfloat16 *__restrict__ dy16, double *loss)
+{
+    __shared__ double part[8];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double e2 = 0.0;
+    if (i < n) {
+        const float e = y[i] - t[i];
+        e2 = (double)e * e;
+        dy[i] = 2.f * e * scale;
+        dy16[i] = __float2bfloat16_rn(2.f * e * scale);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e2 += __shfl_down_sync(0xffffffffu, e2, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = e2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += part[w];
+        atomicAdd(loss, s * scale);
+    }
+}
+
+// db[c] = sum over rows of d[r][c].
+__global__ void k_mlp_colsum(const float *__restrict__ d, int rows, int cols, float *__restrict__ db)
+{
+    const int c = blockIdx.x;
+    float s = 0.f;
+    for (int r = threadIdx.x; r < rows; r += blockDim.x) s += d[(long long)r * cols + c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    __shared__ float part[8];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+        db[c] = t;
+    }
+}
+
+// Adam on the FP32 master parameters; refreshes their BF16 copy.
+__global__ void k_mlp_adam(float *__restrict__ p, const float *__restrict__ gr, float *__restrict__ m,
+                           float *__restrict__ v, __nv_bfloat16 *__restrict__ p16, long long n, float lr, float b1,
+                           float b2, float c1, float c2, float eps)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = gr[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float q = p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    p[i] = q;
+    p16[i] = __float2bfloat16_rn(q);
+}
+
+__global__ void k_to_bf16(const float *__restrict__ x, __nv_bfloat16 *__restrict__ y, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = __float2bfloat16_rn(x[i]);
+}
+
+__global__ void k_gather_rows(const float *__restrict__ src, const int *__restrict__ idx, int rows, int cols,
+                              float *__restrict__ dst)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)rows * cols) return;
+    const long long r = i / cols, c = i - r * cols;
+    dst[i] = src[(long long)idx[r] * cols + c];
+}
+
+unsigned nb(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+int fail(int code, const std::string &m) { return boidsgpu::set_last_error(code, m.c_str()); }
+
+#define MCK(call)                                                                                   \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) return fail(BOIDS_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+}  // namespace
+
+// Parameter layout (FP32 master and BF16 copy): W1 [in x h], b1 [h],
+// W2 [h x h], b2 [h], W3 [h x out], b3 [out]; W row-major (fan-in rows).
+struct boids_mlp {
+    int in = 0, h = 0, out = 0, device = 0;
+    long long np = 0;
+    long long off[6] = {};
+    float *p = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
+    __nv_bfloat16 *p16 = nullptr;
+    long long step = 0;
+    // activations for up to cap rows
+    int cap = 0;
+    float *x = nullptr, *t = nullptr, *pre1 = nullptr, *pre2 = nullptr, *y = nullptr, *dy = nullptr,
+          *d2 = nullptr, *d1 = nullptr;
+    __nv_bfloat16 *x16 = nullptr, *h1 = nullptr, *h2 = nullptr, *dy16 = nullptr, *d2_16 = nullptr, *d1_16 = nullptr;
+    double *loss = nullptr;
+    cudaStream_t st = nullptr;
+};
+
+namespace {
+
+void free_acts(boids_mlp *m)
+{
+    void *q[] = {m->x, m->t, m->pre1, m->pre2, m->y, m->dy, m->d2, m->d1, m->x16, m->h1, m->h2, m->dy16, m->d2_16,
+                 m->d1_16};
+    for (void *p : q)
+        if (p) cudaFree(p);
+    m->x = m->t = m->pre1 = m->pre2 = m->y = m->dy = m->d2 = m->d1 = nullptr;
+    m->x16 = m->h1 = m->h2 = m->dy16 = m->d2_16 = m->d1_16 = nullptr;
+    m->cap = 0;
+}
+
+int ensure_rows(boids_mlp *m, int rows)
+{
+    if (rows <= m->cap) return 0;
+    free_acts(m);
+    const long long r = rows;
+    auto A = [&](auto **p, long long n) { return cudaMalloc((void **)p, sizeof(**p) * (size_t)(n ? n : 1)); };
+    if (A(&m->x, r * m->in) || A(&m->t, r * m->out) || A(&m->pre1, r * m->h) || A(&m->pre2, r * m->h) ||
+        A(&m->y, r * m->out) || A(&m->dy, r * m->out) || A(&m->d2, r * m->h) || A(&m->d1, r * m->h) ||
+        A(&m->x16, r * m->in) || A(&m->h1, r * m->h) || A(&m->h2, r * m->h) || A(&m->dy16, r * m->out) ||
+        A(&m->d2_16, r * m->h) || A(&m->d1_16, r * m->h)) {
+        cudaGetLastError();
+        free_acts(m);
+        return fail(BOIDS_ENOMEM, "boids_mlp: cudaMalloc of activations failed");
+    }
+    m->cap = rows;
+    return 0;
+}
+
+void gemm(boids_mlp *m, MatB A, MatB B, float *C, int ldc, __nv_bfloat16 *C16, int ld16, const float *bias,
+          const float *mask, int ldm, int relu16)
+{
+    dim3 grid(nb(B.cols, kTileN), nb(A.rows, 16 * kWarpsM));
+    k_mlp_gemm<<<grid, 32 * kWarpsM, 0, m->st>>>(A, B, C, ldc, C16, ld16, bias, mask, ldm, relu16);
+}
+
+MatB rowmajor(const __nv_bfloat16 *p, int rows, int cols) { return MatB{p, cols, 1, rows, cols}; }
+MatB transposed(const __nv_bfloat16 *p, int rows, int cols)  // the transpose of a row-major rows x cols
+{
+    return MatB{p, 1, rows == 0 ? 0 : cols, cols, rows};
+}
+
+// Forward pass of `rows` rows already in m->x16; output in m->y.
+void forward(boids_mlp *m, int rows)
+{
+    const __nv_bfloat16 *W1 = m->p16 + m->off[0], *W2 = m->p16 + m->off[2], *W3 = m->p16 + m->off[4];
+    const float *b1 = m->p + m->off[1], *b2 = m->p + m->off[3], *b3 = m->p + m->off[5];
+    gemm(m, rowmajor(m->x16, rows, m->in), rowmajor(W1, m->in, m->h), m->pre1, m->h, m->h1, m->h, b1, nullptr, 0, 1);
+    gemm(m, rowmajor(m->h1, rows, m->h), rowmajor(W2, m->h, m->h), m->pre2, m->h, m->h2, m->h, b2, nullptr, 0, 1);
+    gemm(m, rowmajor(m->h2, rows, m->h), rowmajor(W3, m->h, m->out), m->y, m->out, nullptr, 0, b3, nullptr, 0, 0);
+}
+
+// Loss and gradient of `rows` rows (targets in m->t) into m->grad.
+void backward(boids_mlp *m, int rows)
+{
+    const __nv_bfloat16 *W2 = m->p16 + m->off[2], *W3 = m->p16 + m->off[4];
+    float *gW1 = m->grad + m->off[0], *gb1 = m->grad + m->off[1], *gW2 = m->grad + m->off[2],
+          *gb2 = m->grad + m->off[3], *gW3 = m->grad + m->off[4], *gb3 = m->grad + m->off[5];
+    const int n = rows * m->out;
+    k_mlp_mse<<<nb(n, 256), 256, 0, m->st>>>(m->y, m->t, n, 1.f / (float)n, m->dy, m->dy16, m->loss);
+    // layer 3: dW3 = h2^T dy, db3 = colsum(dy), d2 = (dy W3^T) * (pre2 > 0)
+    gemm(m, transposed(m->h2, rows, m->h), rowmajor(m->dy16, rows, m->out), gW3, m->out, nullptr, 0, nullptr,
+         nullptr, 0, 0);
+    k_mlp_colsum<<<m->out, 256, 0, m->st>>>(m->dy, rows, m->out, gb3);
+    gemm(m, rowmajor(m->dy16, rows, m->out), transposed(W3, m->h, m->out), m->d2, m->h, m->d2_16, m->h, nullptr,
+         m->pre2, m->h, 0);
+    // layer 2
+    gemm(m, transposed(m->h1, rows, m->h), rowmajor(m->d2_16, rows, m->h), gW2, m->h, nullptr, 0, nullptr, nullptr,
+         0, 0);
+    k_mlp_colsum<<<m->h, 256, 0, m->st>>>(m->d2, rows, m->h, gb2);
+    gemm(m, rowmajor(m->d2_16, rows, m->h), transposed(W2, m->h, m->h), m->d1, m->h, m->d1_16, m->h, nullptr,
+         m->pre1, m->h, 0);
+    // layer 1
+    gemm(m, transposed(m->x16, rows, m->in), rowmajor(m->d1_16, rows, m->h), gW1, m->h, nullptr, 0, nullptr, nullptr,
+         0, 0);
+    k_mlp_colsum<<<m->h, 256, 0, m->st>>>(m->d1, rows, m->h, gb1);
+}
+
+int upload_rows(boids_mlp *m, const float *x, const float *t, int rows)
+{
+    MCK(cudaMemcpyAsync(m->x, x, sizeof(float) * (size_t)rows * m->in, cudaMemcpyHostToDevice, m->st));
+    if (t) MCK(cudaMemcpyAsync(m->t, t, sizeof(float) * (size_t)rows * m->out, cudaMemcpyHostToDevice, m->st));
+    k_to_bf16<<<nb((long long)rows * m->in, 256), 256, 0, m->st>>>(m->x, m->x16, (long long)rows * m->in);
+    return 0;
+}
+
+// splitmix64-driven uniform in [-a, a]
+float uni(uint64_t &s, float a)
+{
+    s += 0x9e3779b97f4a7c15ULL;
+    uint64_t z = s;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    z ^= z >> 31;
+    return (float)(((double)(z >> 11) / 9007199254740992.0) * 2.0 - 1.0) * a;
+}
+
+}  // namespace
+
+extern "C" {
+
+int boids_mlp_create(int32_t n_in, int32_t n_hidden, int32_t n_out, uint64_t seed, int32_t device, boids_mlp **out)
+{
+    if (!out || n_in <= 0 || n_hidden <= 0 || n_out <= 0 || n_in > 4096 || n_hidden > 4096 || n_out > 4096)
+        return fail(BOIDS_EINVAL, "boids_mlp_create: bad argument");
+    *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) return fail(BOIDS_ECUDA, "boids_mlp_create: cudaSetDevice");
+    boids_mlp *m = new boids_mlp();
+    m->in = n_in;
+    m->h = n_hidden;
+    m->out = n_out;
+    m->device = device;
+    const long long sz[6] = {(long long)n_in * n_hidden, n_hidden, (long long)n_hidden * n_hidden, n_hidden,
+                             (long long)n_hidden * n_out, n_out};
+    for (int i = 0; i < 6; ++i) {
+        m->off[i] = m->np;
+        m->np += sz[i];
+    }
+    // He-uniform weights, zero biases
+    std::vector<float> h(m->np, 0.f);
+    uint64_t s = seed;
+    const int fan[3] = {n_in, n_hidden, n_hidden};
+    for (int l = 0; l < 3; ++l) {
+        const float a = std::sqrt(6.f / (float)fan[l]);
+        for (long long i = 0; i < sz[2 * l]; ++i) h[m->off[2 * l] + i] = uni(s, a);
+    }
+    bool ok = cudaMalloc(&m->p, 4 * m->np) == cudaSuccess && cudaMalloc(&m->grad, 4 * m->np) == cudaSuccess &&
+              cudaMalloc(&m->m, 4 * m->np) == cudaSuccess && cudaMalloc(&m->v, 4 * m->np) == cudaSuccess &&
+              cudaMalloc(&m->p16, 2 * m->np) == cudaSuccess && cudaMalloc(&m->loss, 8) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaMemcpy(m->p, h.data(), 4 * m->np, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemset(m->m, 0, 4 * m->np) == cudaSuccess && cudaMemset(m->v, 0, 4 * m->np) == cudaSuccess;
+    if (ok) {
+        k_to_bf16<<<nb(m->np, 256), 256, 0, m->st>>>(m->p, m->p16, m->np);
+        ok = cudaStreamSynchronize(m->st) == cudaSuccess;
+    }
+    if (!ok) {
+        cudaGetLastError();
+        boids_mlp_destroy(m);
+        return fail(BOIDS_ENOMEM, "boids_mlp_create: device allocation failed");
+    }
+    *out = m;
+    return BOIDS_OK;
+}
+
+void boids_mlp_destroy(boids_mlp *m)
+{
+    if (!m) return;
+    cudaSetDevice(m->device);
+    if (m->st) cudaStreamSynchronize(m->st);
+    free_acts(m);
+    void *q[] = {m->p, m->grad, m->m, m->v, m->p16, m->loss};
+    for (void *p : q)
+        if (p) cudaFree(p);
+    if (m->st) cudaStreamDestroy(m->st);
+    delete m;
+}
+
+int64_t boids_mlp_param_count(boids_mlp *m) { return m ? m->np : 0; }
+
+int boids_mlp_get_params(boids_mlp *m, float *params)
+{
+    if (!m || !params) return fail(BOIDS_EINVAL, "boids_mlp_get_params: bad argument");
+    cudaSetDevice(m->device);
+    MCK(cudaMemcpyAsync(params, m->p, 4 * m->np, cudaMemcpyDeviceToHost, m->st));
+    MCK(cudaStreamSynchronize(m->st));
+    return BOIDS_OK;
+}
+
+int boids_mlp_set_params(boids_mlp *m, const float *params)
+{
+    if (!m || !params) return fail(BOIDS_EINVAL, "boids_mlp_set_params: bad argument");
+    cudaSetDevice(m->device);
+    MCK(cudaMemcpyAsync(m->p, params, 4 * m->np, cudaMemcpyHostToDevice, m->st));
+    k_to_bf16<<<nb(m->np, 256), 256, 0, m->st>>>(m->p, m->p16, m->np);
+    MCK(cudaMemsetAsync(m->m, 0, 4 * m->np, m->st));
+    MCK(cudaMemsetAsync(m->v, 0, 4 * m->np, m->st));
+    m->step = 0;
+    MCK(cudaStreamSynchronize(m->st));
+    return BOIDS_OK;
+}
+
+int boids_mlp_forward(boids_mlp *m, const float *x, int32_t rows, float *y)
+{
+    if (!m || (!x && rows) || (!y && rows) || rows < 0) return fail(BOIDS_EINVAL, "boids_mlp_forward: bad argument");
+    if (rows == 0) return BOIDS_OK;
+    cudaSetDevice(m->device);
+    if (int rc = ensure_rows(m, rows)) return rc;
+    if (int rc = upload_rows(m, x, nullptr, rows)) return rc;
+    forward(m, rows);
+    MCK(cudaGetLastError());
+    MCK(cudaMemcpyAsync(y, m->y, sizeof(float) * (size_t)rows * m->out, cudaMemcpyDeviceToHost, m->st));
+    MCK(cudaStreamSynchronize(m->st));
+    return BOIDS_OK;
+}
+
+int boids_mlp_gradient(boids_mlp *m, const float *x, const float *t, int32_t rows, float *grad, double *loss)
+{
+    if (!m || !x || !t || !grad || rows <= 0) return fail(BOIDS_EINVAL, "boids_mlp_gradient: bad argument");
+    cudaSetDevice(m->device);
+    if (int rc = ensure_rows(m, rows)) return rc;
+    if (int rc = upload_rows(m, x, t, rows)) return rc;
+    MCK(cudaMemsetAsync(m->loss, 0, 8, m->st));
+    forward(m, rows);
+    backward(m, rows);
+    MCK(cudaGetLastError());
+    MCK(cudaMemcpyAsync(grad, m->grad, 4 * m->np, cudaMemcpyDeviceToHost, m->st));
+    double l = 0;
+    MCK(cudaMemcpyAsync(&l, m->loss, 8, cudaMemcpyDeviceToHost, m->st));
+    MCK(cudaStreamSynchronize(m->st));
+    if (loss) *loss = l;
+    return BOIDS_OK;
+}
+
+int boids_mlp_train(boids_mlp *m, const float *x, const float *t, int32_t rows, int32_t epochs, int32_t batch,
+                    float lr, uint64_t shuffle_seed, double *last_epoch_loss)
+{
+    if (!m || !x || !t || rows <= 0 || epochs < 0 || batch <= 0)
+        return fail(BOIDS_EINVAL, "boids_mlp_train: bad argument");
+    cudaSetDevice(m->device);
+    if (batch > rows) batch = rows;
+    if (int rc = ensure_rows(m, rows + batch)) return rc;
+    // the whole set stays resident: rows [0, rows) of x/t; batches are gathered behind it
+    float *X = m->x, *T = m->t;
+    MCK(cudaMemcpyAsync(X, x, sizeof(float) * (size_t)rows * m->in, cudaMemcpyHostToDevice, m->st));
+    MCK(cudaMemcpyAsync(T, t, sizeof(float) * (size_t)rows * m->out, cudaMemcpyHostToDevice, m->st));
+    int *d_idx = nullptr;
+    float *bx = nullptr, *bt = nullptr;
+    if (cudaMalloc(&d_idx, sizeof(int) * rows) != cudaSuccess ||
+        cudaMalloc(&bx, sizeof(float) * (size_t)batch * m->in) != cudaSuccess ||
+        cudaMalloc(&bt, sizeof(float) * (size_t)batch * m->out) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d_idx);
+        cudaFree(bx);
+        return fail(BOIDS_ENOMEM, "boids_mlp_train: cudaMalloc failed");
+    }
+    std::vector<int> idx(rows);
+    for (int i = 0; i < rows; ++i) idx[i] = i;
+    uint64_t s = shuffle_seed;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    double epoch_loss = 0.0;
+    int rc = 0;
+    float *keep_x = m->x, *keep_t = m->t;
+    for (int ep = 0; ep < epochs && !rc; ++ep) {
+        for (int i = rows - 1; i > 0; --i) {  // Fisher-Yates
+            s += 0x9e3779b97f4a7c15ULL;
+            uint64_t z = s;
+            z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+            z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+            z ^= z >> 31;
+            const int j = (int)(z % (uint64_t)(i + 1));
+            std::swap(idx[i], idx[j]);
+        }
+        if (cudaMemcpyAsync(d_idx, idx.data(), sizeof(int) * rows, cudaMemcpyHostToDevice, m->st) != cudaSuccess ||
+            cudaMemsetAsync(m->loss, 0, 8, m->st) != cudaSuccess) {
+            rc = fail(BOIDS_ECUDA, "boids_mlp_train: copy failed");
+            break;
+        }
+        int nbatch = 0;
+        for (int b0 = 0; b0 < rows; b0 += batch, ++nbatch) {
+            const int r = std::min(batch, rows - b0);
+            k_gather_rows<<<nb((long long)r * m->in, 256), 256, 0, m->st>>>(keep_x, d_idx + b0, r, m->in, bx);
+            k_gather_rows<<<nb((long long)r * m->out, 256), 256, 0, m->st>>>(keep_t, d_idx + b0, r, m->out, bt);
+            // the forward/backward buffers read x/t from m->x/m->t: point them at the batch
+            m->x = bx;
+            m->t = bt;
+            k_to_bf16<<<nb((long long)r * m->in, 256), 256, 0, m->st>>>(bx, m->x16, (long long)r * m->in);
+            forward(m, r);
+            backward(m, r);
+            m->x = keep_x;
+            m->t = keep_t;
+            ++m->step;
+            const float c1 = 1.f - std::pow(b1, (float)m->step), c2 = 1.f - std::pow(b2, (float)m->step);
+            k_mlp_adam<<<nb(m->np, 256), 256, 0, m->st>>>(m->p, m->grad, m->m, m->v, m->p16, m->np, lr, b1, b2, c1,
+                                                         c2, eps);
+        }
+        double l = 0;
+        if (cudaMemcpyAsync(&l, m->loss, 8, cudaMemcpyDeviceToHost, m->st) != cudaSuccess ||
+            cudaStreamSynchronize(m->st) != cudaSuccess) {
+            rc = fail(BOIDS_ECUDA, std::string("boids_mlp_train: ") + cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        epoch_loss = l / nbatch;
+    }
+    if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(BOIDS_ECUDA, "boids_mlp_train: kernel launch failed");
+    cudaFree(d_idx);
+    cudaFree(bx);
+    cudaFree(bt);
+    if (last_epoch_loss) *last_epoch_loss = epoch_loss;
+    return rc;
+}
+
+}  // extern "C"

@@ -89,6 +89,8 @@ size_t layout(const boidsgpu::StepConst &k, unsigned char *base, boidsgpu::DevBu
     b->ticket = reinterpret_cast<uint32_t *>(take(4));
     b->dense_list = reinterpret_cast<uint32_t *>(take(4 * ndense));
     b->dense_n = reinterpret_cast<uint32_t *>(take(8));
+    b->dflag = take(b->ncell / 4);
+    b->carry = nullptr;  // no id windows: cells over the dense list's capacity stay per-boid
     return off;
 }
 
@@ -124,7 +126,6 @@ extern "C" int boids_step_noalloc(const boids_params *params, const float *pos3n
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, params->device);
     b.dense_grid = (uint32_t)(nsm > 0 ? nsm : 1) * 4;
-    b.dense_min = k.dense_min;
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     uint64_t launches = 0;
     // the array keeps the previous call's contents: clear what must start at zero
@@ -133,7 +134,7 @@ extern "C" int boids_step_noalloc(const boids_params *params, const float *pos3n
         (e = boidsgpu::launch_pack(pos3n_in, vel3n_in, b.pos[0], b.vel[0], n, nullptr, 0.f, st, &launches)) ==
             cudaSuccess &&
         (e = boidsgpu::launch_grid_keys(k, b.pos[0], b.key, b.rank, b.count, st, &launches)) == cudaSuccess &&
-        (e = boidsgpu::launch_grid_scan(b, st, &launches)) == cudaSuccess &&
+        (e = boidsgpu::launch_grid_scan(k, b, st, &launches)) == cudaSuccess &&
         (e = boidsgpu::launch_grid_scatter(k, b, 0, true, st, &launches)) == cudaSuccess &&
         (e = boidsgpu::launch_grid_force(k, b, 1, false, false, st, &launches)) == cudaSuccess &&
         (e = boidsgpu::launch_unpack(b.pos[0], b.vel[0], pos3n_out, vel3n_out, n, st, &launches)) ==

@@ -156,6 +156,16 @@ int boids_synchronize(boids_sim *sim);
 int boids_profile_enable(boids_sim *sim, int32_t on);
 int boids_profile_read(boids_sim *sim, boids_profile_t *out, int32_t reset);
 
+/* Which full-size cells the grid engine's CTA-per-cell kernel takes (the
+ * thread-per-boid kernel does the rest; results never depend on it):
+ * tune[0] dense_min   cells holding this many boids or more,
+ * tune[1] defer_min   ... or this many with over
+ * tune[2] cand_defer  candidates in the cell's 27-cell neighbourhood,
+ * tune[3] lone_cand   ... or any boid with over this many candidates.
+ * Defaults 12, 4, 192, 384.  No counterpart in the reference. */
+int boids_set_tuning(boids_sim *sim, const int32_t *tune4);
+int boids_get_tuning(boids_sim *sim, int32_t *tune4);
+
 /* Number of this library's kernels launched by the handle so far. */
 uint64_t boids_kernel_launches(boids_sim *sim);
 
@@ -238,10 +248,36 @@ int boids_ensemble_stats(boids_ensemble *ens, double *out);
  * keep the fastest; results do not depend on the choice.  steps_per_trial
  * <= 0 picks a default.  Leaves the state as it was. */
 int boids_ensemble_autotune(boids_ensemble *ens, int32_t steps_per_trial);
-/* Chosen thresholds: dense_min, defer_min, cand_defer. */
-int boids_ensemble_tuning(boids_ensemble *ens, int32_t *out3);
+/* Chosen thresholds: dense_min, defer_min, cand_defer, lone_cand. */
+int boids_ensemble_tuning(boids_ensemble *ens, int32_t *out4);
 int boids_ensemble_synchronize(boids_ensemble *ens);
 uint64_t boids_ensemble_kernel_launches(boids_ensemble *ens);
+
+/* ------------------------------------------------------------------ sweep surrogate
+ *
+ * A small network that maps a flock's rule parameters to its order
+ * statistics, trained on ensemble runs, to screen parameter sweeps before the
+ * plain simulation re-runs the candidates it selects.  No counterpart in the
+ * reference.  Layers in -> hidden -> hidden -> out with ReLU; BF16 weights
+ * and activations, FP32 accumulation (tensor-core MMA), FP32 master
+ * parameters updated by Adam on the mean squared error.  Parameters are laid
+ * out W1 [in x hidden], b1, W2 [hidden x hidden], b2, W3 [hidden x out], b3,
+ * weight matrices row-major.  Host arrays are row-major, one row per sample. */
+typedef struct boids_mlp boids_mlp;
+int boids_mlp_create(int32_t n_in, int32_t n_hidden, int32_t n_out, uint64_t seed, int32_t device, boids_mlp **out);
+void boids_mlp_destroy(boids_mlp *mlp);
+int64_t boids_mlp_param_count(boids_mlp *mlp);
+int boids_mlp_get_params(boids_mlp *mlp, float *params);
+/* Also resets the optimiser state. */
+int boids_mlp_set_params(boids_mlp *mlp, const float *params);
+int boids_mlp_forward(boids_mlp *mlp, const float *x, int32_t rows, float *y);
+/* One forward and backward pass, no update: the mean squared error and its
+ * gradient with respect to every parameter (same layout as the parameters). */
+int boids_mlp_gradient(boids_mlp *mlp, const float *x, const float *target, int32_t rows, float *grad,
+                       double *loss);
+/* Adam over shuffled mini-batches; *last_epoch_loss = mean batch loss of the last epoch. */
+int boids_mlp_train(boids_mlp *mlp, const float *x, const float *target, int32_t rows, int32_t epochs,
+                    int32_t batch, float lr, uint64_t shuffle_seed, double *last_epoch_loss);
 
 /* Scratch reserved by boids_step_noalloc on every GPU that loads the library. */
 #define BOIDS_NOALLOC_SCRATCH_BYTES (32u << 20)

@@ -153,6 +153,56 @@ def test_dense_cluster_overflow_paths(boids_lib, oracle_mod, engine):
     assert_bits_equal(sim.forces(), of, "forces")
 
 
+def test_huge_cells_in_id_windows(boids_lib, oracle_mod):
+    """Neighbourhoods of thousands of boids (more than the dense kernel's
+    shared list): the cell is done in ascending id windows, its boids' sums
+    carried from window to window, over several rounds of 128 boids."""
+    O = oracle_mod
+    rng = np.random.default_rng(23)
+    n, field = 20000, 1.0
+    prm = O.MARUN2019
+    p = make_params(O, n, field, prm)
+    pos = rng.random((n, 3), dtype=np.float32)
+    ball = rng.permutation(n)[:9000]  # ids spread over the whole range
+    pos[ball] = (0.5 + 0.012 * rng.standard_normal((ball.size, 3))).astype(np.float32)
+    pos[ball[:3000]] = (0.18 + 0.02 * rng.standard_normal((3000, 3))).astype(np.float32)
+    pos = pos.reshape(-1)
+    vel = (0.003 * rng.standard_normal((n, 3))).astype(np.float32).reshape(-1)
+    sim = make_sim(boids_lib, "grid", n, field, prm)
+    sim.set_state(pos, vel)
+    sim.update(2)
+    op, ov, of = _oracle_run(O, p, "grid", pos, vel, 2)
+    gp, gv = sim.state()
+    assert_bits_equal(gp, op, "positions")
+    assert_bits_equal(gv, ov, "velocities")
+    assert_bits_equal(sim.forces(), of, "forces")
+
+
+@pytest.mark.slow
+def test_huge_cell_window_narrowing(boids_lib, oracle_mod):
+    """Over 4096 x 2048 ids in the flock, so one histogram bin of the window
+    search spans more ids than the shared list holds; a ball of consecutive
+    ids makes the first bin overflow and the search narrow to it."""
+    O = oracle_mod
+    rng = np.random.default_rng(29)
+    n = 8_500_000
+    field = float(np.float32((n / 16384.0) ** (1.0 / 3.0)))
+    prm = O.MARUN2019
+    p = make_params(O, n, field, prm)
+    pos = (rng.random((n, 3), dtype=np.float32) * np.float32(field)).astype(np.float32)
+    pos[:2600] = (np.float32(field / 2) + 0.01 * rng.standard_normal((2600, 3))).astype(np.float32)
+    pos = pos.reshape(-1)
+    vel = (0.003 * rng.standard_normal((n, 3))).astype(np.float32).reshape(-1)
+    sim = make_sim(boids_lib, "grid", n, field, prm)
+    sim.set_state(pos, vel)
+    sim.update(1)
+    op, ov, of = _oracle_run(O, p, "grid", pos, vel, 1)
+    gp, gv = sim.state()
+    assert_bits_equal(gp, op, "positions")
+    assert_bits_equal(gv, ov, "velocities")
+    assert_bits_equal(sim.forces(), of, "forces")
+
+
 @pytest.mark.parametrize("engine", ["grid", "allpairs"])
 def test_degenerate_pairs(boids_lib, oracle_mod, engine):
     """Coincident boids (distance 0), zero velocities (0/0 in the cone test),
