@@ -77,6 +77,7 @@ SIGNATURES = {
     "boids_kernel_launches": (C.c_uint64, [_vp]),
     "boids_set_tuning": (C.c_int, [_vp, _vp]),
     "boids_get_tuning": (C.c_int, [_vp, _vp]),
+    "boids_autotune": (C.c_int, [_vp, C.c_int32]),
     "boids_frame_async": (C.c_int, [_vp, _vp, _vp, C.c_int32, C.c_int32]),
     "boids_frame_wait": (C.c_int, [_vp, C.c_int32]),
     "boids_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_vp)]),
@@ -274,6 +275,11 @@ class BoidSimulation:
         t = np.zeros(4, np.int32)
         _check(lib().boids_get_tuning(self.h, _ptr(t)))
         return tuple(int(x) for x in t)
+
+    def autotune(self, steps_per_trial=0):
+        _check(lib().boids_autotune(self.h, steps_per_trial))
+        self._cache = None
+        return self.tuning()
 
     def get_force(self, i):
         return tuple(float(x) for x in self.forces()[i])

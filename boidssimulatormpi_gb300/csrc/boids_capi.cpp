@@ -636,6 +636,76 @@ int boids_get_tuning(boids_sim *s, int32_t *t)
     return BOIDS_OK;
 }
 
+int boids_autotune(boids_sim *s, int32_t steps_per_trial)
+{
+    if (!s) return fail(BOIDS_EINVAL, "boids_autotune: null handle");
+    if (!s->has_state) return fail(BOIDS_ESTATE, "boids_autotune: no state");
+    if (s->engine != 1) return BOIDS_OK;
+    int rc = use_device(s);
+    if (rc) return rc;
+    if (steps_per_trial <= 0) steps_per_trial = 4;
+    const size_t n = s->k.n;
+    float4 *sp = nullptr, *sv = nullptr;
+    if ((rc = dalloc(&sp, n)) || (rc = dalloc(&sv, n))) {
+        if (sp) cudaFree(sp);
+        return rc;
+    }
+    const uint64_t steps_done = s->steps_done;
+    const boids_profile_t acc = s->acc;
+    const bool prof = s->prof;
+    s->prof = false;
+    auto restore = [&]() -> int {
+        CK(cudaMemcpyAsync(s->b.pos[0], sp, sizeof(float4) * n, cudaMemcpyDeviceToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->b.vel[0], sv, sizeof(float4) * n, cudaMemcpyDeviceToDevice, s->stream));
+        s->cur = 0;
+        return grid_bin_fresh(s);
+    };
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (cudaMemcpyAsync(sp, s->b.pos[s->cur], sizeof(float4) * n, cudaMemcpyDeviceToDevice, s->stream) != cudaSuccess ||
+        cudaMemcpyAsync(sv, s->b.vel[s->cur], sizeof(float4) * n, cudaMemcpyDeviceToDevice, s->stream) != cudaSuccess ||
+        cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess)
+        rc = cuda_fail(cudaGetLastError(), "boids_autotune");
+    const StepConst keep = s->k;
+    float best = INFINITY;
+    int best_i = -1;
+    for (int c = 0; !rc && c < boidsgpu::kTuneCount; ++c) {
+        s->k.dense_min = boidsgpu::kTuneCand[c][0];
+        s->k.defer_min = boidsgpu::kTuneCand[c][1];
+        s->k.cand_defer = boidsgpu::kTuneCand[c][2];
+        s->k.lone_cand = boidsgpu::kTuneCand[c][3];
+        if ((rc = restore()) || (rc = boids_step(s, 1))) break;  // one warm-up update
+        float ms = 0.f;
+        if (cudaEventRecord(t0, s->stream) != cudaSuccess || (rc = boids_step(s, steps_per_trial)) ||
+            cudaEventRecord(t1, s->stream) != cudaSuccess || cudaEventSynchronize(t1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, t0, t1) != cudaSuccess) {
+            if (!rc) rc = cuda_fail(cudaGetLastError(), "boids_autotune timing");
+            break;
+        }
+        if (ms < best) {
+            best = ms;
+            best_i = c;
+        }
+    }
+    s->k = keep;
+    if (!rc && best_i >= 0) {
+        s->k.dense_min = boidsgpu::kTuneCand[best_i][0];
+        s->k.defer_min = boidsgpu::kTuneCand[best_i][1];
+        s->k.cand_defer = boidsgpu::kTuneCand[best_i][2];
+        s->k.lone_cand = boidsgpu::kTuneCand[best_i][3];
+    }
+    int rc2 = restore();
+    if (!rc2 && cudaStreamSynchronize(s->stream) != cudaSuccess) rc2 = cuda_fail(cudaGetLastError(), "boids_autotune");
+    s->steps_done = steps_done;
+    s->acc = acc;
+    s->prof = prof;
+    s->forces_valid = false;
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+    cudaFree(sp);
+    cudaFree(sv);
+    return rc ? rc : rc2;
+}
+
 int boids_frame_async(boids_sim *s, float *pframe, float *vframe, int32_t with_forces, int32_t slot)
 {
     if (!s || !pframe || slot < 0 || slot >= BOIDS_FRAME_SLOTS)

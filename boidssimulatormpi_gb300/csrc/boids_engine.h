@@ -108,11 +108,25 @@ struct DevBuffers {
 
 constexpr int kScanTile = 2048;       // cells per scan block (256 threads x 8)
 constexpr int kListCap = 32;          // grid engine, sparse cells: sorted neighbours kept per pass
+// Defaults: best for uniform flocks with a cold L2 (at N = 2^20, lower
+// thresholds cost 25 % there, as every dense cell's gather-and-sort chain
+// then waits on DRAM); gathered flocks run up to 15 % faster with lower
+// ones, which the autotuners pick.
 constexpr int kDenseMin = 12;         // default dense_min
 constexpr int kDeferMin = 4;          // default defer_min
 constexpr int kCandDefer = 192;       // default cand_defer
 constexpr int kLoneCand = 384;        // default lone_cand
 constexpr int kCarryBytes = 72;       // partial sums of one boid between id windows
+
+// Dense-cell threshold sets the autotuners try, {dense_min, defer_min,
+// cand_defer, lone_cand}; the first is the default.  Crowded (clustered)
+// states favour low thresholds, uniform states high ones.
+constexpr uint32_t kNever = 1u << 30;
+constexpr uint32_t kTuneCand[][4] = {
+    {12, 4, 192, 384}, {8, 2, 96, 128}, {8, 4, 128, 256}, {6, 3, 96, 192},
+    {4, 2, 64, 128}, {16, 4, 256, 512}, {12, 4, 192, 2048}, {kNever, kNever, kNever, 1024},
+};
+constexpr int kTuneCount = sizeof(kTuneCand) / sizeof(kTuneCand[0]);
 
 // Entries the dense-cell work list can need in one step: each non-empty
 // full-size cell (4 x cells) is listed at most once.
@@ -121,7 +135,7 @@ inline size_t dense_list_capacity(size_t ncell, size_t n)
     const size_t by_cells = ncell / 4;
     return (by_cells < n ? by_cells : n) + 1;
 }
-constexpr int kDenseCap = 2048;       // candidates of a dense cell held in shared memory
+constexpr int kDenseCap = 1024;       // candidates of a dense cell held in shared memory
 constexpr int kApCap = 64;            // all-pairs engine: neighbours kept per boid
 constexpr uint32_t kMaxBoids = 1u << 29;  // slot index packs into 29 bits
 

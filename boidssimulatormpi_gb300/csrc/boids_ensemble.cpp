@@ -49,14 +49,6 @@ int cuda_fail(cudaError_t e, const char *where)
 
 constexpr int kGraphSteps = 16;  // steps per captured graph
 
-// Dense-cell threshold candidates tried by the autotuner:
-// {dense_min, defer_min, cand_defer, lone_cand}; the first is the default.
-constexpr uint32_t kNever = 1u << 30;
-constexpr uint32_t kTuneCand[][4] = {
-    {12, 4, 192, 384}, {8, 4, 128, 256}, {16, 4, 256, 512}, {24, 6, 384, 768}, {6, 3, 96, 192},
-    {12, 4, 192, 2048}, {kNever, kNever, kNever, 1024},
-};
-
 }  // namespace
 
 struct boids_ensemble {
@@ -502,8 +494,8 @@ int boids_ensemble_autotune(boids_ensemble *e, int32_t steps_per_trial)
         rc = cuda_fail(cudaGetLastError(), "boids_ensemble_autotune");
     uint32_t keep[4];
     std::memcpy(keep, e->tune, sizeof keep);
-    for (size_t c = 0; !rc && c < sizeof(kTuneCand) / sizeof(kTuneCand[0]); ++c) {
-        std::memcpy(e->tune, kTuneCand[c], sizeof e->tune);
+    for (int c = 0; !rc && c < boidsgpu::kTuneCount; ++c) {
+        std::memcpy(e->tune, boidsgpu::kTuneCand[c], sizeof e->tune);
         if ((rc = upload_table(e)) || (rc = restore()) || (rc = step_once(e))) break;  // one warm-up step
         if (cudaEventRecord(t0, e->stream) != cudaSuccess) { rc = cuda_fail(cudaGetLastError(), "cudaEventRecord"); break; }
         for (int t = 0; t < steps_per_trial && !rc; ++t) rc = step_once(e);
@@ -519,7 +511,7 @@ int boids_ensemble_autotune(boids_ensemble *e, int32_t steps_per_trial)
             best_i = (int)c;
         }
     }
-    if (!rc) std::memcpy(e->tune, kTuneCand[best_i], sizeof e->tune);
+    if (!rc) std::memcpy(e->tune, boidsgpu::kTuneCand[best_i], sizeof e->tune);
     else std::memcpy(e->tune, keep, sizeof e->tune);
     int rc2 = upload_table(e);
     if (!rc2) rc2 = restore();

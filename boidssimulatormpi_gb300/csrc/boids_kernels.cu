@@ -635,8 +635,33 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
     const StepConst &k = MULTI ? kf : kp;
     const int G = k.G, Gx = k.Gx;
     const int t = threadIdx.x;
-    const uint32_t s = blockIdx.x * kRT + t;
-    bool act = s - k.slot_base < k.n;
+    // This CTA's boids outside dense cells (the others are k_grid_dense's),
+    // compacted onto its first threads so that warps run full and the
+    // warps left over exit at once.
+    __shared__ uint32_t cslot[kRT];
+    __shared__ uint32_t wcount[kRT / 32];
+    const uint32_t s0 = blockIdx.x * kRT + t;
+    bool mine = s0 - k.slot_base < k.n;
+    if (mine) {
+        const float4 q = g.pos[s0];
+        const uint32_t fc = k.cell_base / 4 +
+                            (uint32_t)((cell1(q.z, k) * G + cell1(q.y, k)) * G + cell1(q.x, k));
+        mine = !__ldg(g.dflag + fc);
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, mine);
+    const int lane = t & 31, wid = t >> 5;
+    if (lane == 0) wcount[wid] = __popc(bal);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+#pragma unroll
+    for (int i = 0; i < kRT / 32; ++i) {
+        if (i < wid) before += wcount[i];
+        total += wcount[i];
+    }
+    if (mine) cslot[before + __popc(bal & ((1u << lane) - 1u))] = s0;
+    __syncthreads();
+    bool act = (uint32_t)t < total;
+    const uint32_t s = act ? cslot[t] : s0;
     const float4 p4 = act ? g.pos[s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 v4 = act ? g.vel[s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float3 pi = xyz(p4), vi = xyz(v4);
@@ -648,8 +673,6 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
         yy = yy < 0 ? yy + G : (yy >= G ? yy - G : yy);
         return k.cell_base + (uint32_t)(zz * G + yy) * (uint32_t)Gx;
     };
-    // boids of dense cells are k_grid_dense's
-    if (act && __ldg(g.dflag + row_base(4) / 4 + (uint32_t)cx)) act = false;
     // This boid's segments: in each neighbour row, the x cells that a sphere
     // of radius sqrt(trim_r2) around it reaches.
     int nseg = 0;
@@ -834,6 +857,7 @@ struct DenseSmem {
     uint32_t work, flock;
     uint32_t nw, cut;              // huge cells: window size, histogram cut
     uint32_t wtot[kDT / 32];       // block scan scratch
+    float4 svel[kDenseCap];        // candidates' velocities, id order
     StepConst kf;  // the current cell's flock (batched ensembles)
 };
 static_assert(kDenseCap <= 2048, "gather index must fit 11 bits");
@@ -863,7 +887,7 @@ __device__ __forceinline__ float3 cand_image(float4 c, float3 pi, const float4 *
 // running count passes kDenseCap; if the first bin alone is over, the span
 // narrows to that bin.  A boid is a candidate at most once (G >= 3), so a
 // bin one id wide always fits and the search ends.
-constexpr int kWinBins = 4096;
+constexpr int kWinBins = 2048;
 
 __device__ uint32_t dense_window(DenseSmem &sm, const GridIn &g, int ns, uint32_t lo, uint32_t nid)
 {
@@ -1028,6 +1052,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                     sm.u.spos[q0 + i] = wrapped ? make_float4(p.x + sh[0], p.y + sh[1], p.z + sh[2],
                                                               __uint_as_float(slot_r[i] | 0x80000000u))
                                                 : make_float4(p.x, p.y, p.z, __uint_as_float(slot_r[i]));
+                    sm.svel[q0 + i] = __ldg(g.vel + slot_r[i]);
                 }
             }
             __syncthreads();
@@ -1070,7 +1095,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                             const int f = pair_flags(pi, sight, tt, k);
                             if (!f) continue;
                             if (l == 0) {
-                                const float3 vj = (f & 4) ? xyz(__ldg(g.vel + j)) : make_float3(0.f, 0.f, 0.f);
+                                const float3 vj = (f & 4) ? xyz(sm.svel[q]) : make_float3(0.f, 0.f, 0.f);
                                 acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
                             } else if (nl < kChunkList) {
                                 sm.v.lists[t * kChunkList + nl++] = q | ((uint32_t)f << 16);
@@ -1099,7 +1124,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                                 const float3 tt = cand_image(cq, pi, g.pos, k);
                                 const int f = pair_flags(pi, sight, tt, k);
                                 if (!f) continue;
-                                const float3 vj = (f & 4) ? xyz(__ldg(g.vel + j)) : make_float3(0.f, 0.f, 0.f);
+                                const float3 vj = (f & 4) ? xyz(sm.svel[q]) : make_float3(0.f, 0.f, 0.f);
                                 acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
                             }
                         } else {
@@ -1110,7 +1135,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                                 const int f = (int)(v >> 16);
                                 const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
                                 const float3 tt = cand_image(cq, pi, g.pos, k);
-                                const float3 vj = (f & 4) ? xyz(__ldg(g.vel + j)) : make_float3(0.f, 0.f, 0.f);
+                                const float3 vj = (f & 4) ? xyz(sm.svel[v & 0xffffu]) : make_float3(0.f, 0.f, 0.f);
                                 acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
                             }
                         }

@@ -15,7 +15,7 @@
 //  * the array holds BOIDS_NOALLOC_SCRATCH_BYTES (32 MiB) on every GPU that
 //    loads the library, used or not, until the process exits;
 //  * a step that needs more scratch than that is refused with BOIDS_EINVAL
-//    (about 440 000 boids at the reference's density);
+//    (about 370 000 boids at the reference's density);
 //  * all calls share the one array: two calls whose GPU work overlaps in time
 //    (different streams, or different host threads on one device) race and
 //    corrupt each other's results; order them on one stream.

@@ -59,21 +59,24 @@ def flocks(u: np.ndarray, n_boids: int, seed: int, device: int = 0):
 
 
 def simulate(u: np.ndarray, n_boids: int, steps: int, seed: int = 12345, chunk: int = 8192,
-             autotune: bool = True) -> tuple[np.ndarray, float]:
+             retune: bool = True) -> tuple[np.ndarray, float]:
     """Order statistics (polarization, milling, NN distance, largest cluster)
     of every point after `steps` updates, and the seconds the GPU spent
-    (create/init excluded, synchronised wall time of the steps and stats)."""
+    (create/init excluded, synchronised wall time of the steps, a retuning of
+    the dense-cell thresholds a quarter of the way in, and the statistics)."""
     u = np.atleast_2d(u)
     stats = np.empty((u.shape[0], 4))
     gpu_s = 0.0
     for c0 in range(0, u.shape[0], chunk):
         ens = Ensemble(flocks(u[c0:c0 + chunk], n_boids, seed))
         ens.init()
-        if autotune and steps >= 64:
-            ens.autotune()
         ens.synchronize()
         t0 = time.perf_counter()
-        ens.step(steps)
+        q = steps // 4 if retune and steps >= 200 else 0
+        if q:
+            ens.step(q)
+            ens.autotune(2)
+        ens.step(steps - q)
         st = ens.stats()
         gpu_s += time.perf_counter() - t0
         stats[c0:c0 + chunk] = st[:, :4]
@@ -123,3 +126,55 @@ def screened_sweep(screen: Screen, u: np.ndarray, frac: float, n_boids: int, ste
 
 def recall(chosen: np.ndarray, truth: np.ndarray) -> float:
     return len(set(chosen.tolist()) & set(truth.tolist())) / max(1, len(truth))
+
+
+def run(n_boids=2048, steps=300, n_train=1024, n_sweep=8192, frac=0.02, oversample=(1, 2, 4), epochs=300,
+        seed=12345, noise_points=64):
+    """Plain sweep vs surrogate-screened sweep on the same Latin hypercube;
+    returns a dict of times, the surrogate's error, and the recall of the
+    plain sweep's top `frac` set for each statistic."""
+    ut = latin_hypercube(n_train, seed=1)
+    us = latin_hypercube(n_sweep, seed=2)
+    st_train, gpu_train = simulate(ut, n_boids, steps, seed)
+    st_plain, gpu_plain = simulate(us, n_boids, steps, seed)
+    # the statistics' own spread from the initial placement alone
+    st_other, _ = simulate(us[:noise_points], n_boids, steps, seed + 1)
+    sc = Screen()
+    loss, fit_s = sc.fit(ut, st_train, epochs=epochs)
+    t0 = time.perf_counter()
+    pred = sc.predict(us)
+    infer_s = time.perf_counter() - t0
+    out = {"n_boids": n_boids, "steps": steps, "train_points": n_train, "sweep_points": n_sweep, "frac": frac,
+           "gpu_s": {"train_simulations": gpu_train, "plain_sweep": gpu_plain, "fit": fit_s, "inference": infer_s},
+           "fit_loss": loss, "objectives": {}}
+    for o, name in enumerate(OBJECTIVES):
+        truth = top(st_plain[:, o], frac)
+        res = {"corr": float(np.corrcoef(pred[:, o], st_plain[:, o])[0, 1]),
+               "rmse": float(np.sqrt(np.mean((pred[:, o] - st_plain[:, o]) ** 2))),
+               "spread": float(st_plain[:, o].std()),
+               "seed_noise": float((st_other[:, o] - st_plain[:noise_points, o]).std() / np.sqrt(2)),
+               "recall": {}}
+        for m in oversample:
+            pick = top(pred[:, o], frac * m)
+            _, sim_s = simulate(us[pick], n_boids, steps, seed)
+            res["recall"]["x%d" % m] = {"recall": recall(pick, truth), "resimulated": int(pick.size),
+                                        "gpu_s": infer_s + sim_s,
+                                        "fraction_of_plain": (infer_s + sim_s) / gpu_plain}
+        out["objectives"][name] = res
+    sc.close()
+    return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="plain vs surrogate-screened parameter sweep")
+    ap.add_argument("--boids", type=int, default=2048)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--train", type=int, default=1024)
+    ap.add_argument("--sweep", type=int, default=8192)
+    ap.add_argument("--frac", type=float, default=0.02)
+    ap.add_argument("--epochs", type=int, default=300)
+    a = ap.parse_args()
+    print(json.dumps(run(a.boids, a.steps, a.train, a.sweep, a.frac, epochs=a.epochs)))

@@ -166,6 +166,14 @@ int boids_profile_read(boids_sim *sim, boids_profile_t *out, int32_t reset);
 int boids_set_tuning(boids_sim *sim, const int32_t *tune4);
 int boids_get_tuning(boids_sim *sim, int32_t *tune4);
 
+/* Time a few updates with each candidate threshold set on a copy of the
+ * current state, keep the fastest, and put the state back (grid engine; a
+ * no-op for the all-pairs engine).  Crowded flocks favour other thresholds
+ * than uniform ones, so long runs may call it again as the flock gathers.
+ * get_force values of the last update are lost.  steps_per_trial <= 0 picks
+ * a default.  No counterpart in the reference. */
+int boids_autotune(boids_sim *sim, int32_t steps_per_trial);
+
 /* Number of this library's kernels launched by the handle so far. */
 uint64_t boids_kernel_launches(boids_sim *sim);
 
@@ -294,7 +302,7 @@ int boids_mlp_train(boids_mlp *mlp, const float *x, const float *target, int32_t
  *
  * All scratch lives in one static device array of BOIDS_NOALLOC_SCRATCH_BYTES
  * that every GPU loading the library holds until the process exits; a step
- * needing more (roughly 440 000 boids at the reference's density) returns
+ * needing more (roughly 370 000 boids at the reference's density) returns
  * BOIDS_EINVAL.  The first call on a device looks up the array's device
  * address, so make that first call before any stream capture.  Every call
  * shares the array: calls whose GPU work overlaps (other streams, other

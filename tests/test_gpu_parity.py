@@ -180,9 +180,10 @@ def test_huge_cells_in_id_windows(boids_lib, oracle_mod):
 
 @pytest.mark.slow
 def test_huge_cell_window_narrowing(boids_lib, oracle_mod):
-    """Over 4096 x 2048 ids in the flock, so one histogram bin of the window
-    search spans more ids than the shared list holds; a ball of consecutive
-    ids makes the first bin overflow and the search narrow to it."""
+    """More ids in the flock than the window search's bins times the shared
+    list's capacity (2048 x 1024), so one histogram bin spans more ids than
+    the list holds; a ball of consecutive ids makes the first bin overflow
+    and the search narrow to it."""
     O = oracle_mod
     rng = np.random.default_rng(29)
     n = 8_500_000
@@ -341,3 +342,51 @@ def test_host_init_reproduces_reference_golden(boids_lib, oracle_mod, path):
     gp, gv = sim.state()
     assert_bits_equal(gp, g["pos0"], "initial positions")
     assert_bits_equal(gv, g["vel0"], "initial velocities")
+
+
+@pytest.mark.parametrize("tuning", [(1, 1, 0, 0), (1 << 30, 1 << 30, 1 << 30, 1 << 30), (4, 2, 64, 128)])
+def test_dense_thresholds_do_not_change_results(boids_lib, oracle_mod, tuning):
+    """Every cell to the CTA-per-cell kernel, every boid to the per-boid
+    kernel (cells over the shared list still go dense, in id windows), and a
+    mix: the same bits as the oracle."""
+    O = oracle_mod
+    rng = np.random.default_rng(41)
+    n, field = 6000, 0.9
+    prm = O.MARUN2019
+    p = make_params(O, n, field, prm)
+    pos = rng.random((n, 3), dtype=np.float32) * np.float32(field)
+    pos[:2500] = (0.45 + 0.03 * rng.standard_normal((2500, 3))).astype(np.float32)
+    pos = pos.reshape(-1)
+    vel = (0.003 * rng.standard_normal((n, 3))).astype(np.float32).reshape(-1)
+    sim = make_sim(boids_lib, "grid", n, field, prm)
+    sim.set_tuning(*tuning)
+    assert sim.tuning() == tuple(tuning)
+    sim.set_state(pos, vel)
+    sim.update(3)
+    op, ov, of = _oracle_run(O, p, "grid", pos, vel, 3)
+    gp, gv = sim.state()
+    assert_bits_equal(gp, op, "positions")
+    assert_bits_equal(gv, ov, "velocities")
+    assert_bits_equal(sim.forces(), of, "forces")
+
+
+def test_handle_autotune_keeps_the_trajectory(boids_lib, oracle_mod):
+    O = oracle_mod
+    prm = O.MARUN2019
+    n, field = 20000, 1.08
+    a = make_sim(boids_lib, "grid", n, field, prm)
+    b = make_sim(boids_lib, "grid", n, field, prm)
+    for s in (a, b):
+        s.init()
+        s.update(40)
+    t = a.autotune(2)
+    assert len(t) == 4
+    pa, va = a.state()
+    pb, vb = b.state()
+    assert_bits_equal(pa, pb, "state after autotune")
+    a.update(25)
+    b.update(25)
+    pa, va = a.state()
+    pb, vb = b.state()
+    assert_bits_equal(pa, pb, "positions")
+    assert_bits_equal(va, vb, "velocities")
