@@ -108,10 +108,9 @@ struct DevBuffers {
 
 constexpr int kScanTile = 2048;       // cells per scan block (256 threads x 8)
 constexpr int kListCap = 32;          // grid engine, sparse cells: sorted neighbours kept per pass
-// Defaults: best for uniform flocks with a cold L2 (at N = 2^20, lower
-// thresholds cost 25 % there, as every dense cell's gather-and-sort chain
-// then waits on DRAM); gathered flocks run up to 15 % faster with lower
-// ones, which the autotuners pick.
+// Defaults: best for the first tens of steps from a uniform start (at
+// N = 2^20, lower thresholds cost 25 % there); gathered flocks run up to
+// 25 % faster with lower ones, which the autotuners pick.
 constexpr int kDenseMin = 12;         // default dense_min
 constexpr int kDeferMin = 4;          // default defer_min
 constexpr int kCandDefer = 192;       // default cand_defer
