@@ -157,6 +157,14 @@ struct boids_sim {
     // completion event per slot, made on first use
     float *frame_dev = nullptr;
     cudaEvent_t frame_ev[BOIDS_FRAME_SLOTS] = {};
+    // kGraphSteps updates captured into a CUDA graph on first use; valid for
+    // the stream, buffer parity and constants it was captured with
+    cudaGraphExec_t graph = nullptr;
+    cudaStream_t graph_stream = nullptr;
+    int graph_cur = -1;
+    StepConst graph_k{};
+    uint64_t graph_launches = 0;  // kernel launches per replay
+    bool graph_off = false;       // capture failed once on this handle
 };
 
 namespace {
@@ -485,6 +493,7 @@ void boids_destroy(boids_sim *s)
     cudaSetDevice(s->p.device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_buffers(s->b);
+    if (s->graph) cudaGraphExecDestroy(s->graph);
     if (s->frame_dev) cudaFree(s->frame_dev);
     for (cudaEvent_t e : s->frame_ev)
         if (e) cudaEventDestroy(e);
@@ -556,6 +565,81 @@ int boids_init_ex(boids_sim *s, const char *init, int32_t seed, int32_t seed_mod
 
 int boids_init(boids_sim *s, const char *init, int32_t seed) { return boids_init_ex(s, init, seed, -1); }
 
+namespace {
+
+constexpr int kGraphSteps = 16;  // updates per captured graph
+
+// One update: BoidSimulation::update of the grid or all-pairs engine.
+int step_once(boids_sim *s, bool rec)
+{
+    if (s->engine == 1) {
+        {
+            PhaseTimer pt(s, 0);
+            CK(boidsgpu::launch_grid_scan(s->k, s->b, s->stream, &s->launches));
+            CK(boidsgpu::launch_grid_scatter(s->k, s->b, s->cur, true, s->stream, &s->launches));
+            s->acc.bin_launches += 2;
+        }
+        PhaseTimer pt(s, 1);
+        CK(boidsgpu::launch_grid_force(s->k, s->b, 1 - s->cur, false, rec, s->stream, &s->launches));
+        s->acc.force_launches += 1;
+    } else {
+        PhaseTimer pt(s, 1);
+        CK(boidsgpu::launch_allpairs(s->k, s->b, s->cur, false, rec, s->stream, &s->launches));
+        s->cur = 1 - s->cur;
+        s->acc.force_launches += 2;
+    }
+    s->acc.steps++;
+    s->steps_done++;
+    return 0;
+}
+
+// The graph of kGraphSteps updates for the handle's current stream, buffer
+// parity and constants, captured if needed; false when it cannot be had.
+bool graph_ready(boids_sim *s, bool rec)
+{
+    if (s->graph_off || !s->stream) return false;  // the legacy stream cannot be captured
+    if (s->graph && s->graph_stream == s->stream && s->graph_cur == s->cur &&
+        std::memcmp(&s->graph_k, &s->k, sizeof(StepConst)) == 0)
+        return true;
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    if (boidsgpu::grid_prepare() != cudaSuccess) {  // function attributes are set outside the capture
+        cudaGetLastError();
+        s->graph_off = true;
+        return false;
+    }
+    const uint64_t launches = s->launches, done = s->steps_done;
+    const boids_profile_t acc = s->acc;
+    const int cur = s->cur;
+    cudaGraph_t g = nullptr;
+    bool ok = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    for (int t = 0; ok && t < kGraphSteps; ++t) ok = step_once(s, rec) == 0;
+    if (cudaStreamEndCapture(s->stream, &g) != cudaSuccess) ok = false;
+    s->graph_launches = s->launches - launches;
+    s->launches = launches;
+    s->steps_done = done;
+    s->acc = acc;
+    s->cur = cur;  // nothing ran: only recorded
+    if (ok && cudaGraphInstantiate(&s->graph, g, 0) != cudaSuccess) {
+        s->graph = nullptr;
+        ok = false;
+    }
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+        cudaGetLastError();
+        s->graph_off = true;
+        return false;
+    }
+    s->graph_stream = s->stream;
+    s->graph_cur = s->cur;
+    s->graph_k = s->k;
+    return true;
+}
+
+}  // namespace
+
 int boids_step(boids_sim *s, int32_t steps)
 {
     if (!s || steps < 0) return fail(BOIDS_EINVAL, "boids_step: bad argument");
@@ -563,26 +647,18 @@ int boids_step(boids_sim *s, int32_t steps)
     int rc = use_device(s);
     if (rc) return rc;
     const bool rec = s->b.forces != nullptr;
-    for (int32_t t = 0; t < steps; ++t) {
-        if (s->engine == 1) {
-            {
-                PhaseTimer pt(s, 0);
-                CK(boidsgpu::launch_grid_scan(s->k, s->b, s->stream, &s->launches));
-                CK(boidsgpu::launch_grid_scatter(s->k, s->b, s->cur, true, s->stream, &s->launches));
-                s->acc.bin_launches += 2;
-            }
-            PhaseTimer pt(s, 1);
-            CK(boidsgpu::launch_grid_force(s->k, s->b, 1 - s->cur, false, rec, s->stream, &s->launches));
-            s->acc.force_launches += 1;
-        } else {
-            PhaseTimer pt(s, 1);
-            CK(boidsgpu::launch_allpairs(s->k, s->b, s->cur, false, rec, s->stream, &s->launches));
-            s->cur = 1 - s->cur;
-            s->acc.force_launches += 2;
+    int32_t t = 0;
+    // long runs replay captured graphs (not while timing phases with events)
+    if (steps >= 2 * kGraphSteps && !s->prof && graph_ready(s, rec)) {
+        for (; steps - t >= kGraphSteps; t += kGraphSteps) {
+            CK(cudaGraphLaunch(s->graph, s->stream));
+            s->launches += s->graph_launches;
+            s->steps_done += kGraphSteps;
+            s->acc.steps += kGraphSteps;
         }
-        s->acc.steps++;
-        s->steps_done++;
     }
+    for (; t < steps; ++t)
+        if ((rc = step_once(s, rec))) return rc;
     if (steps > 0) s->forces_valid = rec;
     return BOIDS_OK;
 }

@@ -96,8 +96,8 @@ struct DevBuffers {
     int32_t *cells8;           // 8 per boid (id order)
     int32_t *dcnt;             // 3 per boid (id order)
     uint64_t *dhash;           // 3 per boid (id order)
-    uint32_t *dense_list;      // full-size cells for the dense kernel, this step (dense_list_capacity)
-    uint32_t *dense_n;         // their number, then the dense kernel's work queue (2 words)
+    uint32_t *dense_list;      // dense kernel work items (cell, first boid), this step (dense_list_capacity words)
+    uint32_t *dense_n;         // the number of items, then the dense kernel's work queue (2 words)
     uint8_t *dflag;            // per full-size cell: 1 when the dense kernel takes it
     void *carry;               // per slot, kCarryBytes: partial sums between id windows (null: no windows)
     uint32_t *flag;            // set_state range check (1 word)
@@ -127,12 +127,16 @@ constexpr uint32_t kTuneCand[][4] = {
 };
 constexpr int kTuneCount = sizeof(kTuneCand) / sizeof(kTuneCand[0]);
 
-// Entries the dense-cell work list can need in one step: each non-empty
-// full-size cell (4 x cells) is listed at most once.
+// The dense kernel's work items are (full-size cell, first boid) pairs, one
+// per kDenseRound boids of a dense cell, so that the boids of one crowded
+// cell spread over several CTAs.  Words the work list can need in one step:
+// at most one item per non-empty cell plus one per kDenseRound boids, two
+// words per item.
+constexpr int kDenseRound = 128;
 inline size_t dense_list_capacity(size_t ncell, size_t n)
 {
     const size_t by_cells = ncell / 4;
-    return (by_cells < n ? by_cells : n) + 1;
+    return 2 * ((by_cells < n ? by_cells : n) + n / kDenseRound + 1);
 }
 constexpr int kDenseCap = 1024;       // candidates of a dense cell held in shared memory
 constexpr int kApCap = 64;            // all-pairs engine: neighbours kept per boid

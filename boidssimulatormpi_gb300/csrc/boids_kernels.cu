@@ -583,7 +583,12 @@ __global__ void k_grid_classify(const uint32_t *__restrict__ count, const uint32
         }
         if (dense_rule(b, ncand, k, windows)) {
             flag = 1;
-            dense_list[atomicAdd(dense_n, 1u)] = cg;
+            const uint32_t items = (b + kDenseRound - 1) / kDenseRound;
+            const uint32_t at = atomicAdd(dense_n, items);
+            for (uint32_t r = 0; r < items; ++r) {
+                dense_list[2 * (at + r)] = cg;
+                dense_list[2 * (at + r) + 1] = r * kDenseRound;
+            }
         }
     }
     dflag[cg] = flag;
@@ -873,14 +878,6 @@ __device__ __forceinline__ float3 cand_image(float4 c, float3 pi, const float4 *
     return xyz(c);
 }
 
-// One CTA takes one crowded cell at a time (dynamic queue).  The cell's
-// 27-cell candidates are radix-sorted by id once.  The cell's b boids x the
-// candidate list is then split over all threads: each boid gets L = 128/b
-// lanes, lane l walks chunk l of the id-ordered list; chunk 0's lane (the
-// owner) accumulates its accepted neighbours at once, the others hand theirs
-// over in id order and the owner folds them in after its own, so the
-// accumulation order stays ascending id.  A chunk lane whose hand-over list
-// overflows leaves its chunk to the owner.
 // Id window of a huge cell (more than kDenseCap candidates): the largest hi
 // such that the candidates with ids in [lo, hi) fit the shared list.  A
 // histogram of the candidates' ids over kWinBins bins is cut where the
@@ -933,10 +930,11 @@ __device__ uint32_t dense_window(DenseSmem &sm, const GridIn &g, int ns, uint32_
     }
 }
 
-// One CTA takes one crowded cell at a time (dynamic queue).  The cell's
-// 27-cell candidates are radix-sorted by id once.  The cell's b boids x the
-// candidate list is then split over all threads: each boid gets L = 128/b
-// lanes, lane l walks chunk l of the id-ordered list; chunk 0's lane (the
+// One CTA takes one work item at a time (dynamic queue): a crowded cell and
+// up to 128 of its boids (a cell with more boids is several items, taken by
+// several CTAs).  The cell's 27-cell candidates are radix-sorted by id once
+// per item.  The item's b boids x the candidate list is then split over all
+// threads: each boid gets L = 128/b lanes, lane l walks chunk l of the id-ordered list; chunk 0's lane (the
 // owner) accumulates its accepted neighbours at once, the others hand theirs
 // over in id order and the owner folds them in after its own, so the
 // accumulation order stays ascending id.  A chunk lane whose hand-over list
@@ -956,7 +954,8 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
         __syncthreads();
         const uint32_t w = sm.work;
         if (w >= dense_n[0]) break;
-        const uint32_t cg = dense_list[w];  // global full-size cell
+        const uint32_t cg = dense_list[2 * w];        // global full-size cell
+        const uint32_t rbeg = dense_list[2 * w + 1];  // the item's first boid of the cell
         if (MULTI) {
             if (t == 0) {  // the flock: last with cell4 <= cg
                 uint32_t lo = 0, hi = ft.count;
@@ -1058,7 +1057,8 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
             __syncthreads();
             const bool first = lo == 0, last = hi >= k.n;
 
-            for (uint32_t r0 = 0; r0 < b; r0 += kDT) {
+            static_assert(kDenseRound == kDT, "a work item is one round of boids");
+            for (uint32_t r0 = rbeg; r0 < min(b, rbeg + (uint32_t)kDenseRound); r0 += kDT) {
                 const uint32_t nbr = min(b - r0, (uint32_t)kDT);      // boids this round
                 const uint32_t L = (uint32_t)kDT / nbr;               // lanes per boid
                 const uint32_t csz = (nw + L - 1) / L;                // chunk length

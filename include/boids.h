@@ -118,7 +118,9 @@ int boids_init_ex(boids_sim *sim, const char *initialization, int32_t rand_seed,
 int boids_set_state(boids_sim *sim, const float *pos3n, const float *vel3n);
 
 /* BoidSimulation::update (src/boid_simulation_grid.cpp:165-293), `steps`
- * times.  Asynchronous on the handle's stream. */
+ * times.  Asynchronous on the handle's stream.  A call of 32 or more steps
+ * captures 16 updates into a CUDA graph once (per stream, buffer parity and
+ * tuning) and replays it; results are the same bits either way. */
 int boids_step(boids_sim *sim, int32_t steps);
 
 /* BoidSimulation::get(id, &x,&y,&z, &vx,&vy,&vz) for every id

@@ -390,3 +390,32 @@ def test_handle_autotune_keeps_the_trajectory(boids_lib, oracle_mod):
     pb, vb = b.state()
     assert_bits_equal(pa, pb, "positions")
     assert_bits_equal(va, vb, "velocities")
+
+
+@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+def test_graph_replayed_steps_equal_single_steps(boids_lib, oracle_mod, engine):
+    """boids_step(sim, k >= 32) replays captured 16-update graphs; the same
+    updates one call at a time give the same bits and the same launch count."""
+    O = oracle_mod
+    prm = O.MARUN2019
+    n, field = (12000, 0.91) if engine == "grid" else (3000, 0.6)
+    a = make_sim(boids_lib, engine, n, field, prm)
+    b = make_sim(boids_lib, engine, n, field, prm)
+    for s in (a, b):
+        s.init()
+    la, lb = a.kernel_launches(), b.kernel_launches()
+    a.update(70)          # 4 graph replays + 6 direct updates
+    for _ in range(70):
+        b.update(1)
+    pa, va = a.state()
+    pb, vb = b.state()
+    assert_bits_equal(pa, pb, "positions")
+    assert_bits_equal(va, vb, "velocities")
+    assert_bits_equal(a.forces(), b.forces(), "forces")
+    assert a.kernel_launches() - la == b.kernel_launches() - lb
+    a.set_tuning(4, 2, 64, 128)  # new constants: the graph is captured again
+    b.set_tuning(4, 2, 64, 128)
+    a.update(40)
+    for _ in range(40):
+        b.update(1)
+    assert_bits_equal(a.state()[0], b.state()[0], "positions after retuning")
