@@ -108,13 +108,15 @@ struct DevBuffers {
 
 constexpr int kScanTile = 2048;       // cells per scan block (256 threads x 8)
 constexpr int kListCap = 32;          // grid engine, sparse cells: sorted neighbours kept per pass
-// Defaults: best for the first tens of steps from a uniform start (at
-// N = 2^20, lower thresholds cost 25 % there); gathered flocks run up to
-// 25 % faster with lower ones, which the autotuners pick.
+// Defaults: the lowest thresholds that keep the first tens of steps from a
+// uniform start at full speed (at N = 2^20, lone_cand 64 or dense_min 8
+// cost 25 % to 4x there, as many small cells become CTA work items).
+// Gathered flocks run up to 2x faster with lone_cand 96 than 384 and
+// another 20 % with lower values still, which the autotuners pick.
 constexpr int kDenseMin = 12;         // default dense_min
 constexpr int kDeferMin = 4;          // default defer_min
 constexpr int kCandDefer = 192;       // default cand_defer
-constexpr int kLoneCand = 384;        // default lone_cand
+constexpr int kLoneCand = 96;         // default lone_cand
 constexpr int kCarryBytes = 72;       // partial sums of one boid between id windows
 
 // Dense-cell threshold sets the autotuners try, {dense_min, defer_min,
@@ -122,8 +124,8 @@ constexpr int kCarryBytes = 72;       // partial sums of one boid between id win
 // states favour low thresholds, uniform states high ones.
 constexpr uint32_t kNever = 1u << 30;
 constexpr uint32_t kTuneCand[][4] = {
-    {12, 4, 192, 384}, {8, 2, 96, 128}, {8, 4, 128, 256}, {6, 3, 96, 192},
-    {4, 2, 64, 128}, {16, 4, 256, 512}, {12, 4, 192, 2048}, {kNever, kNever, kNever, 1024},
+    {12, 4, 192, 96}, {12, 4, 192, 384}, {12, 4, 192, 64}, {12, 4, 192, 48},
+    {8, 2, 96, 128}, {4, 2, 64, 128}, {8, 4, 128, 64}, {kNever, kNever, kNever, 1024},
 };
 constexpr int kTuneCount = sizeof(kTuneCand) / sizeof(kTuneCand[0]);
 
