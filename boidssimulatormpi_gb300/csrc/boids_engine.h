@@ -107,7 +107,7 @@ struct DevBuffers {
 };
 
 constexpr int kScanTile = 2048;       // cells per scan block (256 threads x 8)
-constexpr int kListCap = 32;          // grid engine, sparse cells: sorted neighbours kept per pass
+constexpr int kListCap = 12;          // grid engine, thread-per-boid kernel: sorted neighbours kept per pass
 // Defaults: the lowest thresholds that keep the first tens of steps from a
 // uniform start at full speed (at N = 2^20, lone_cand 64 or dense_min 8
 // cost 25 % to 4x there, as many small cells become CTA work items).

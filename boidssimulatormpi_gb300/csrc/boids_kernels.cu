@@ -610,7 +610,7 @@ __global__ void k_grid_classify(const uint32_t *__restrict__ count, const uint32
 // buffer, sorted list) live in shared memory, one column per thread: as
 // local memory they overflow L1 and every access goes to L2.
 constexpr int kBufA = 12;
-constexpr int kListA = 12;
+constexpr int kListA = kListCap;
 constexpr int kRT = 128;      // threads of k_grid_sparse
 constexpr int kSegA = 18;     // at most 9 rows x 2 runs (a run split where x wraps)
 
@@ -1158,8 +1158,8 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
 // rejects almost all pairs; survivors get the exact tests and accepted
 // neighbours are appended to the boid's list (unordered).
 constexpr int kApThreads = 128;
-constexpr int kApKI = 4;                        // i per thread
-constexpr int kApTileI = kApThreads * kApKI;    // 512
+constexpr int kApKI = 8;                        // i per thread
+constexpr int kApTileI = kApThreads * kApKI;    // 1024
 constexpr int kApTileJ = 1024;
 
 __global__ void __launch_bounds__(kApThreads)
