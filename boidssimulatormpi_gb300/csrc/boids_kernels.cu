@@ -623,8 +623,8 @@ struct GridIn {
 };
 
 struct SparseSmem {
-    uint32_t seg0[kSegA][kRT];   // first slot | x-shift code << 29 | (row >> 3) << 31
-    uint32_t seg1[kSegA][kRT];   // end slot | (row & 7) << 29
+    uint32_t seg0[kSegA][kRT];   // first slot | x shift << 29 | (z shift < 0) << 31
+    uint32_t seg1[kSegA][kRT];   // end slot   | y shift << 29 | (z shift > 0) << 31
     uint32_t buf[kBufA][kRT];    // filter hits: slot | shifted << 31
     uint64_t lst[kListA][kRT];   // accepted neighbours, sorted: id << 32 | slot | flags << 29
 };
@@ -697,24 +697,31 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
             const int lo = __float2int_rd((pi.x - rx) * k.inv_subx);
             const int hi = __float2int_rd((pi.x + rx) * k.inv_subx);
             int a0 = lo, a1 = hi + 1, c0 = 0, c1 = 0;  // x-cell runs [a0, a1) and [c0, c1)
-            uint32_t ca = 0, cb = 0;                     // x-shift codes: 1 = -F, 2 = +F
-            if (lo < 0) { a0 = lo + Gx; a1 = Gx; ca = 1; c1 = min(hi + 1, Gx); }
-            else if (hi >= Gx) { a1 = Gx; c1 = hi + 1 - Gx; cb = 2; }
+            uint32_t ca = 0, cb = 0;  // x shifts of the runs, 2-bit two's complement: 3 = -F, 1 = +F
+            if (lo < 0) { a0 = lo + Gx; a1 = Gx; ca = 3; c1 = min(hi + 1, Gx); }
+            else if (hi >= Gx) { a1 = Gx; c1 = hi + 1 - Gx; cb = 1; }
             const uint32_t rb = row_base(r);
-            const uint32_t rhi = (uint32_t)(r >> 3) << 31, rlo = (uint32_t)(r & 7) << 29;
+            // y and z shifts of the row, as the x shifts
+            const uint32_t ysh = cy + dy < 0 ? 3u : (cy + dy >= G ? 1u : 0u);
+            const uint32_t w0 = cz + dz < 0 ? 0x80000000u : 0u, w1 = (ysh << 29) | (cz + dz >= G ? 0x80000000u : 0u);
+            // empty runs are not stored: a stored segment always has a candidate
             if (a1 > a0) {
                 const uint32_t j0 = slot_start(g.lstart, g.bsum, rb + a0, k), j1 = slot_start(g.lstart, g.bsum, rb + a1, k);
-                sm.seg0[nseg][t] = j0 | (ca << 29) | rhi;
-                sm.seg1[nseg][t] = j1 | rlo;
-                ncand += j1 - j0;
-                ++nseg;
+                if (j1 > j0) {
+                    sm.seg0[nseg][t] = j0 | (ca << 29) | w0;
+                    sm.seg1[nseg][t] = j1 | w1;
+                    ncand += j1 - j0;
+                    ++nseg;
+                }
             }
             if (c1 > c0) {
                 const uint32_t j0 = slot_start(g.lstart, g.bsum, rb + c0, k), j1 = slot_start(g.lstart, g.bsum, rb + c1, k);
-                sm.seg0[nseg][t] = j0 | (cb << 29) | rhi;
-                sm.seg1[nseg][t] = j1 | rlo;
-                ncand += j1 - j0;
-                ++nseg;
+                if (j1 > j0) {
+                    sm.seg0[nseg][t] = j0 | (cb << 29) | w0;
+                    sm.seg1[nseg][t] = j1 | w1;
+                    ncand += j1 - j0;
+                    ++nseg;
+                }
             }
         }
     }
@@ -737,19 +744,18 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
         const uint32_t mine = need ? nc : 0;
         for (uint32_t it = 0; it < max_nc; ++it) {
             if (it < mine) {
-                while (j == jend) {  // next non-empty segment
+                if (j == jend) {  // next segment (none is empty)
                     ++qs;
                     const uint32_t w0 = sm.seg0[qs][t], w1 = sm.seg1[qs][t];
                     j = w0 & 0x1fffffffu;
                     jend = w1 & 0x1fffffffu;
-                    const int r = (int)(((w0 >> 31) << 3) | (w1 >> 29));
-                    const uint32_t code = (w0 >> 29) & 3u;
-                    const int dz = r / 3 - 1, dy = r % 3 - 1;
-                    const float sx = code == 1 ? -k.Ff : (code == 2 ? k.Ff : 0.f);
-                    const float sy = cy + dy < 0 ? -k.Ff : (cy + dy >= G ? k.Ff : 0.f);
-                    const float sz = cz + dz < 0 ? -k.Ff : (cz + dz >= G ? k.Ff : 0.f);
-                    qx = pi.x - sx; qy = pi.y - sy; qz = pi.z - sz;
-                    swrap = (code != 0 || sy != 0.f || sz != 0.f) ? 0x80000000u : 0u;
+                    // the candidate's image is pj + shift: test pj against pi - shift
+                    const int vx = (int)(w0 << 1) >> 30, vy = (int)(w1 << 1) >> 30;
+                    const int vz = (int)(w1 >> 31) - (int)(w0 >> 31);
+                    qx = __fmaf_rn(-__int2float_rn(vx), k.Ff, pi.x);
+                    qy = __fmaf_rn(-__int2float_rn(vy), k.Ff, pi.y);
+                    qz = __fmaf_rn(-__int2float_rn(vz), k.Ff, pi.z);
+                    swrap = ((w0 | w1) & 0xe0000000u) ? 0x80000000u : 0u;
                 }
                 const float4 pj = __ldg(g.pos + j);
                 const float dx = pj.x - qx, dy = pj.y - qy, dz = pj.z - qz;
