@@ -369,6 +369,14 @@ int make_constants(const boids_params &p, StepConst &k, bool *ref_ok)
     const double rf = (double)rmax * (1.0 + 1e-4) + 8.0 * ulpF;
     k.filt_r2 = (float)(rf * rf);
     k.box_lim = (float)(p.field_size / 2 - rf * (1.0 + 1e-4) - 8.0 * ulpF);
+    // The filters' relative vector differs from the exact imaged one by a
+    // few ulps of the coordinates (at most 2F in magnitude), each dot
+    // product by those times |v|_1 <= sqrt(3)|v| plus three roundings of
+    // |v| * |r|: 64 ulps and 1e-5 * rf per unit |v| bound both with room.
+    k.dot_eps = (float)(64.0 * ulpF + 1e-5 * rf);
+    k.cone_pre = 1;
+    for (int r = 0; r < 3; ++r)
+        if (k.rule[r].all_round || !(k.rule[r].cstar > 0.f)) k.cone_pre = 0;
 
     // reference overlapping-grid geometry
     float refR = 0.f, refGS = 0.f;

@@ -49,6 +49,12 @@ struct StepConst {
     float vmax_f, vmin_f;    // speed clamp scale factors (float)vmax, (float)vmin
     float d2_any;        // largest d2_lim of the three rules
     float cone_band;     // approximate cone tests closer than this to a threshold are redone exactly
+    // View-cone pre-test of the candidate filters, on when every rule has a
+    // cone that rejects c <= 0 (cstar > 0): a candidate whose approximate
+    // v . r is below -|v| * dot_eps has an exact v . r < 0 and fails all
+    // three rules.  dot_eps bounds the approximation's error per unit |v|.
+    float dot_eps;
+    int32_t cone_pre;
     int32_t id_bits;     // bits needed for the largest boid id, rounded up to a multiple of 4
     RuleConst rule[3];   // cohesion, separation, alignment
     // the reference's overlapping grid, for Boid::grid_index parity

@@ -730,6 +730,7 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
     if (max_nc == 0) return;  // the whole warp is idle
 
     const Sight sight = make_sight(vi);
+    const float dot_lim = k.cone_pre ? -(sight.nv * k.dot_eps) : -INFINITY;  // cone pre-test
     Acc a;
     acc_zero(a);
     int64_t lo_id = -1;  // ids <= lo_id were accumulated by earlier passes
@@ -760,7 +761,8 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
                 const float4 pj = __ldg(g.pos + j);
                 const float dx = pj.x - qx, dy = pj.y - qy, dz = pj.z - qz;
                 const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                if (d2 < k.filt_r2 && j != s) sm.buf[nb++][t] = j | swrap;
+                const float dv = __fmaf_rn(vi.z, dz, __fmaf_rn(vi.y, dy, __fmul_rn(vi.x, dx)));
+                if (d2 < k.filt_r2 && dv >= dot_lim && j != s) sm.buf[nb++][t] = j | swrap;
                 ++j;
             }
             // exact tests of the buffered hits, the whole warp together
@@ -1075,6 +1077,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                 const float4 p4 = g.pos[s], v4 = g.vel[s];
                 const float3 pi = xyz(p4), vi = xyz(v4);
                 const Sight sight = make_sight(vi);
+                const float dot_lim = k.cone_pre ? -(sight.nv * k.dot_eps) : -INFINITY;  // cone pre-test
                 Acc a;
                 if (act && l == 0 && !first) a = o.carry[s];  // the earlier windows' sums
                 else acc_zero(a);
@@ -1088,7 +1091,8 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                         const float4 cq = sm.u.spos[q];
                         const float dx = cq.x - pi.x, dy = cq.y - pi.y, dz = cq.z - pi.z;
                         const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                        if (d2 < k.filt_r2) sm.bufs[nb++ * kDT + t] = (uint16_t)q;
+                        const float dv = __fmaf_rn(vi.z, dz, __fmaf_rn(vi.y, dy, __fmul_rn(vi.x, dx)));
+                        if (d2 < k.filt_r2 && dv >= dot_lim) sm.bufs[nb++ * kDT + t] = (uint16_t)q;
                     }
                     // exact tests of the buffered hits, the whole warp together
                     if (__any_sync(0xffffffffu, nb == kBufB) || it + 1 == maxlen) {
@@ -1125,8 +1129,9 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                                 const float4 cq = sm.u.spos[q];
                                 const float dx = cq.x - pi.x, dy = cq.y - pi.y, dz = cq.z - pi.z;
                                 const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                                const float dv = __fmaf_rn(vi.z, dz, __fmaf_rn(vi.y, dy, __fmul_rn(vi.x, dx)));
                                 const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
-                                if (!(d2 < k.filt_r2) || j == s) continue;
+                                if (!(d2 < k.filt_r2) || !(dv >= dot_lim) || j == s) continue;
                                 const float3 tt = cand_image(cq, pi, g.pos, k);
                                 const int f = pair_flags(pi, sight, tt, k);
                                 if (!f) continue;

@@ -231,6 +231,62 @@ def test_degenerate_pairs(boids_lib, oracle_mod, engine):
     assert_bits_equal(sim.forces(), of, "forces")
 
 
+def _perpendicular_groups(n_groups, field, seed):
+    """Groups of 8 boids: a centre and 7 neighbours placed at right angles
+    to the centre's velocity, give or take a few ulps, so that the exact
+    v . r of many pairs is 0 or within rounding of it; a quarter of the
+    groups straddle a periodic face."""
+    rng = np.random.default_rng(seed)
+    pos, vel = [], []
+    for g in range(n_groups):
+        c = rng.random(3) * field
+        if g % 4 == 0:
+            c[g // 4 % 3] = field * rng.choice([0.0, 0.9995, 0.0004])
+        v = rng.standard_normal(3)
+        v *= rng.uniform(0.001, 0.005) / np.linalg.norm(v)
+        vh = v / np.linalg.norm(v)
+        pos.append(c)
+        vel.append(v)
+        for k in range(7):
+            u = np.cross(vh, rng.standard_normal(3))
+            u /= np.linalg.norm(u)
+            eps = rng.choice([0.0, 1e-9, -1e-9, 3e-8, -3e-8, 1e-7, -1e-7])
+            pos.append(np.mod(c + rng.uniform(0.003, 0.0499) * u + eps * vh, field))
+            vel.append(rng.standard_normal(3) * 0.003)
+    pos = np.asarray(pos, np.float32)
+    pos[pos >= np.float32(field)] = 0.0
+    return pos, np.asarray(vel, np.float32)
+
+
+@pytest.mark.parametrize("tuning", [None, (1 << 30, 1 << 30, 1 << 30, 1 << 30), (1, 1, 0, 0)],
+                         ids=["default", "all_sparse", "all_dense"])
+def test_view_cone_pretest_at_right_angles(boids_lib, oracle_mod, tuning):
+    """The candidate filters drop pairs behind a boid (approximate v . r
+    below -|v| * dot_eps) before the exact tests; pairs at right angles to
+    the velocity, within rounding of v . r = 0, are the ones that pre-test
+    could get wrong.  Neighbour sets, forces and the next state must equal
+    the oracle's."""
+    O = oracle_mod
+    field = 1.0
+    pos, vel = _perpendicular_groups(512, field, 23)
+    n = pos.shape[0]
+    prm = dict(O.MARUN2019)
+    p = make_params(O, n, field, prm)
+    sim = make_sim(boids_lib, "grid", n, field, prm)
+    if tuning:
+        sim.set_tuning(*tuning)
+    sim.set_state(pos, vel)
+    cnt, hsh = sim.neighbor_sets()
+    ocnt, ohsh = O.neighbor_sets(p, pos.reshape(-1), vel.reshape(-1))
+    assert np.array_equal(cnt, ocnt) and np.array_equal(hsh, ohsh)
+    sim.update(2)
+    op, ov, of = _oracle_run(O, p, "allpairs", pos.reshape(-1), vel.reshape(-1), 2)
+    gp, gv = sim.state()
+    assert_bits_equal(gp, op, "positions")
+    assert_bits_equal(gv, ov, "velocities")
+    assert_bits_equal(sim.forces(), of, "forces")
+
+
 def test_all_round_angles_and_test_ini(boids_lib, oracle_mod):
     """Sight angles >= 1 skip the cone test entirely (src/boid.cpp:29-31)."""
     O = oracle_mod
