@@ -844,7 +844,12 @@ __device__ uint64_t *block_radix_sort(uint64_t *a, uint64_t *b, uint32_t *hist, 
 
 constexpr int kDT = 128;                       // threads of k_grid_dense
 constexpr int kBufB = 16;                      // filter hits buffered per lane
-constexpr int kChunkList = 32;                 // accepted neighbours a chunk lane hands to its owner
+// Accepted neighbours the chunk lanes hand to their owners, 16-bit entries
+// (index | flags << 13).  The owners (chunk 0) keep theirs in registers, so
+// the kChunkPool entries are split over the nbr x (L - 1) other lanes:
+// kChunkPool / (nbr (L - 1)) >= 64 each, 128 when two lanes share a boid.
+constexpr int kChunkPool = 8192;
+static_assert(kDenseCap <= (1 << 13), "a list entry holds the candidate index in 13 bits");
 constexpr int kDenseKT = kDenseCap / kDT;      // candidates per thread when the list is full
 
 // Shared memory of k_grid_dense.  Regions whose lifetimes do not overlap
@@ -860,7 +865,7 @@ struct DenseSmem {
             uint32_t gslot[kDenseCap];      // state slot, by gather index
             uint32_t hist[16 * kDT];
         } s;
-        uint32_t lists[kDT * kChunkList];   // (index | flags << 16) per chunk lane
+        uint16_t lists[kChunkPool];         // per non-owner chunk lane: index | flags << 13
     } v;
     uint16_t bufs[kBufB * kDT];
     uint16_t nlist[kDT];
@@ -1073,6 +1078,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                 const bool act = (uint32_t)t < nbr * L;
                 const uint32_t bi = act ? (uint32_t)t % nbr : 0, l = act ? (uint32_t)t / nbr : 0;
                 const uint32_t k0 = act ? min(nw, l * csz) : 0, k1 = act ? min(nw, k0 + csz) : 0;
+                const uint32_t lcap = L > 1 ? (uint32_t)kChunkPool / (nbr * (L - 1)) : 0;  // list entries per lane
                 const uint32_t s = own0 + r0 + bi;
                 const float4 p4 = g.pos[s], v4 = g.vel[s];
                 const float3 pi = xyz(p4), vi = xyz(v4);
@@ -1107,8 +1113,8 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                             if (l == 0) {
                                 const float3 vj = (f & 4) ? xyz(sm.svel[q]) : make_float3(0.f, 0.f, 0.f);
                                 acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
-                            } else if (nl < kChunkList) {
-                                sm.v.lists[t * kChunkList + nl++] = q | ((uint32_t)f << 16);
+                            } else if ((uint32_t)nl < lcap) {
+                                sm.v.lists[(t - nbr) * lcap + nl++] = (uint16_t)(q | ((uint32_t)f << 13));
                             } else {
                                 ovf = true;
                             }
@@ -1141,12 +1147,12 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                         } else {
                             const uint32_t m = sm.nlist[tt_];
                             for (uint32_t e = 0; e < m; ++e) {
-                                const uint32_t v = sm.v.lists[tt_ * kChunkList + e];
-                                const float4 cq = sm.u.spos[v & 0xffffu];
-                                const int f = (int)(v >> 16);
+                                const uint32_t v = sm.v.lists[(tt_ - nbr) * lcap + e];
+                                const float4 cq = sm.u.spos[v & 0x1fffu];
+                                const int f = (int)(v >> 13);
                                 const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
                                 const float3 tt = cand_image(cq, pi, g.pos, k);
-                                const float3 vj = (f & 4) ? xyz(sm.svel[v & 0xffffu]) : make_float3(0.f, 0.f, 0.f);
+                                const float3 vj = (f & 4) ? xyz(sm.svel[v & 0x1fffu]) : make_float3(0.f, 0.f, 0.f);
                                 acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
                             }
                         }
