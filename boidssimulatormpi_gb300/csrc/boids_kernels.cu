@@ -810,7 +810,11 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
 
 // Stable LSD radix sort of n 64-bit keys held in shared memory, on bits
 // [lo, lo + nbits), 4 bits per pass; NT threads each own a contiguous run.
-// Returns the buffer that holds the sorted keys.
+// hist holds 17 * NT words: counter i lives at i + i / 16, so that both the
+// (digit, thread) column walks and the thread-contiguous scan are free of
+// bank conflicts.  Returns the buffer that holds the sorted keys.
+__device__ __forceinline__ int hpad(int i) { return i + (i >> 4); }
+
 template <int NT>
 __device__ uint64_t *block_radix_sort(uint64_t *a, uint64_t *b, uint32_t *hist, int n, int lo, int nbits)
 {
@@ -820,21 +824,21 @@ __device__ uint64_t *block_radix_sort(uint64_t *a, uint64_t *b, uint32_t *hist, 
     const int i0 = min(n, t * K), i1 = min(n, i0 + K);
     for (int bit = lo; bit < lo + nbits; bit += 4) {
 #pragma unroll
-        for (int d = 0; d < 16; ++d) hist[d * NT + t] = 0;
-        for (int i = i0; i < i1; ++i) hist[((uint32_t)(a[i] >> bit) & 15u) * NT + t]++;
+        for (int d = 0; d < 16; ++d) hist[hpad(d * NT + t)] = 0;
+        for (int i = i0; i < i1; ++i) hist[hpad((int)((uint32_t)(a[i] >> bit) & 15u) * NT + t)]++;
         __syncthreads();
         // exclusive scan of hist in (digit, thread) order; thread t owns 16 entries
         uint32_t loc[16], sum = 0;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) { loc[q] = hist[16 * t + q]; sum += loc[q]; }
+        for (int q = 0; q < 16; ++q) { loc[q] = hist[17 * t + q]; sum += loc[q]; }
         uint32_t total;
         uint32_t pre = block_excl_scan<NT>(sum, wsum, total);
 #pragma unroll
-        for (int q = 0; q < 16; ++q) { hist[16 * t + q] = pre; pre += loc[q]; }
+        for (int q = 0; q < 16; ++q) { hist[17 * t + q] = pre; pre += loc[q]; }
         __syncthreads();
         for (int i = i0; i < i1; ++i) {
             const uint64_t v = a[i];
-            b[hist[((uint32_t)(v >> bit) & 15u) * NT + t]++] = v;
+            b[hist[hpad((int)((uint32_t)(v >> bit) & 15u) * NT + t)]++] = v;
         }
         __syncthreads();
         uint64_t *tmp = a; a = b; b = tmp;
@@ -848,6 +852,7 @@ constexpr int kBufB = 16;                      // filter hits buffered per lane
 // (index | flags << 13).  The owners (chunk 0) keep theirs in registers, so
 // the kChunkPool entries are split over the nbr x (L - 1) other lanes:
 // kChunkPool / (nbr (L - 1)) >= 64 each, 128 when two lanes share a boid.
+// Entries are interleaved across lanes (entry-major).
 constexpr int kChunkPool = 8192;
 static_assert(kDenseCap <= (1 << 13), "a list entry holds the candidate index in 13 bits");
 constexpr int kDenseKT = kDenseCap / kDT;      // candidates per thread when the list is full
@@ -863,7 +868,7 @@ struct DenseSmem {
     union {
         struct {
             uint32_t gslot[kDenseCap];      // state slot, by gather index
-            uint32_t hist[16 * kDT];
+            uint32_t hist[17 * kDT];        // radix counters, padded (block_radix_sort)
         } s;
         uint16_t lists[kChunkPool];         // per non-owner chunk lane: index | flags << 13
     } v;
@@ -1043,13 +1048,13 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
             const uint64_t *sorted =
                 block_radix_sort<kDT>(sm.u.keys[0], sm.u.keys[1], sm.v.s.hist, (int)nw, 16, k.id_bits);
             // lay the candidates out in id order over the dead sort buffers
-            const int K = ((int)nw + kDT - 1) / kDT;
-            const int q0 = t * K;
+            // (thread t takes positions t, t + kDT, ...: no bank conflicts)
             uint32_t slot_r[kDenseKT], seg_r[kDenseKT];
 #pragma unroll
             for (int i = 0; i < kDenseKT; ++i) {
-                if (i < K && q0 + i < (int)nw) {
-                    const uint64_t key = sorted[q0 + i];
+                const int q = t + i * kDT;
+                if (q < (int)nw) {
+                    const uint64_t key = sorted[q];
                     slot_r[i] = sm.v.s.gslot[(uint32_t)key & 0x7ffu];
                     seg_r[i] = ((uint32_t)key >> 11) & 0x1fu;
                 }
@@ -1057,14 +1062,15 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
             __syncthreads();
 #pragma unroll
             for (int i = 0; i < kDenseKT; ++i) {
-                if (i < K && q0 + i < (int)nw) {
+                const int q = t + i * kDT;
+                if (q < (int)nw) {
                     const float4 p = __ldg(g.pos + slot_r[i]);
                     const float *sh = sm.seg_s[seg_r[i]];
                     const bool wrapped = sh[0] != 0.f || sh[1] != 0.f || sh[2] != 0.f;
-                    sm.u.spos[q0 + i] = wrapped ? make_float4(p.x + sh[0], p.y + sh[1], p.z + sh[2],
-                                                              __uint_as_float(slot_r[i] | 0x80000000u))
-                                                : make_float4(p.x, p.y, p.z, __uint_as_float(slot_r[i]));
-                    sm.svel[q0 + i] = __ldg(g.vel + slot_r[i]);
+                    sm.u.spos[q] = wrapped ? make_float4(p.x + sh[0], p.y + sh[1], p.z + sh[2],
+                                                         __uint_as_float(slot_r[i] | 0x80000000u))
+                                           : make_float4(p.x, p.y, p.z, __uint_as_float(slot_r[i]));
+                    sm.svel[q] = __ldg(g.vel + slot_r[i]);
                 }
             }
             __syncthreads();
@@ -1078,7 +1084,9 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                 const bool act = (uint32_t)t < nbr * L;
                 const uint32_t bi = act ? (uint32_t)t % nbr : 0, l = act ? (uint32_t)t / nbr : 0;
                 const uint32_t k0 = act ? min(nw, l * csz) : 0, k1 = act ? min(nw, k0 + csz) : 0;
-                const uint32_t lcap = L > 1 ? (uint32_t)kChunkPool / (nbr * (L - 1)) : 0;  // list entries per lane
+                // list entries per non-owner lane; entry e of lane x = t - nbr sits at
+                // e * lw + x, so that lanes side by side use banks side by side
+                const uint32_t lw = nbr * (L - 1), lcap = L > 1 ? (uint32_t)kChunkPool / lw : 0;
                 const uint32_t s = own0 + r0 + bi;
                 const float4 p4 = g.pos[s], v4 = g.vel[s];
                 const float3 pi = xyz(p4), vi = xyz(v4);
@@ -1114,7 +1122,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                                 const float3 vj = (f & 4) ? xyz(sm.svel[q]) : make_float3(0.f, 0.f, 0.f);
                                 acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
                             } else if ((uint32_t)nl < lcap) {
-                                sm.v.lists[(t - nbr) * lcap + nl++] = (uint16_t)(q | ((uint32_t)f << 13));
+                                sm.v.lists[nl++ * lw + (t - nbr)] = (uint16_t)(q | ((uint32_t)f << 13));
                             } else {
                                 ovf = true;
                             }
@@ -1147,7 +1155,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                         } else {
                             const uint32_t m = sm.nlist[tt_];
                             for (uint32_t e = 0; e < m; ++e) {
-                                const uint32_t v = sm.v.lists[(tt_ - nbr) * lcap + e];
+                                const uint32_t v = sm.v.lists[e * lw + (tt_ - nbr)];
                                 const float4 cq = sm.u.spos[v & 0x1fffu];
                                 const int f = (int)(v >> 13);
                                 const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
