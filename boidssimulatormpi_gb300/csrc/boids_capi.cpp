@@ -173,9 +173,12 @@ void free_buffers(DevBuffers &b)
 {
     void *ptrs[] = {b.pos[0], b.pos[1], b.vel[0], b.vel[1], b.key, b.rank, b.count, b.lstart,
                     b.bsum, b.ticket, b.ap_cnt, b.ap_list, b.forces, b.stage, b.cells8, b.dcnt, b.dhash,
-                    b.dense_list, b.dense_n, b.flag, b.dflag, b.carry};
+                    b.dense_list, b.dense_n, b.flag, b.dflag, b.carry, b.defer};
     for (void *q : ptrs)
         if (q) cudaFree(q);
+    if (b.aux) cudaStreamDestroy(b.aux);
+    if (b.fork) cudaEventDestroy(b.fork);
+    if (b.join) cudaEventDestroy(b.join);
     b = DevBuffers{};
 }
 
@@ -473,7 +476,16 @@ int boids_create(const boids_params *params, boids_sim **out)
             ALLOC(&carry, (size_t)boidsgpu::kCarryBytes * n);
             b.carry = carry;
         }
-        ALLOC(&b.dense_n, 2, true);
+        ALLOC(&b.dense_n, 3, true);
+        ALLOC(&b.defer, 2 * n);
+        if (cudaStreamCreateWithFlags(&b.aux, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b.join, cudaEventDisableTiming) != cudaSuccess) {
+            const cudaError_t ce = cudaGetLastError();
+            free_buffers(b);
+            delete s;
+            return cuda_fail(ce, "cudaStreamCreate (side stream)");
+        }
         int nsm = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p.device);
         b.dense_grid = (uint32_t)std::max(1, nsm) * 4;

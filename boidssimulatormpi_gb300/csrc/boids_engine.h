@@ -103,7 +103,12 @@ struct DevBuffers {
     int32_t *dcnt;             // 3 per boid (id order)
     uint64_t *dhash;           // 3 per boid (id order)
     uint32_t *dense_list;      // dense kernel work items (cell, first boid), this step (dense_list_capacity words)
-    uint32_t *dense_n;         // the number of items, then the dense kernel's work queue (2 words)
+    uint32_t *dense_n;         // dense items, the dense kernel's work queue, deferred sparse boids (3 words)
+    uint32_t *defer;           // sparse boids deferred to further passes: (slot, lo_id), 2 words per boid (null: none)
+    // Side stream on which the deferred boids run beside the dense kernel,
+    // forked from and joined back to the engine's stream (null: in order).
+    cudaStream_t aux;
+    cudaEvent_t fork, join;
     uint8_t *dflag;            // per full-size cell: 1 when the dense kernel takes it
     void *carry;               // per slot, kCarryBytes: partial sums between id windows (null: no windows)
     uint32_t *flag;            // set_state range check (1 word)

@@ -264,7 +264,7 @@ int boids_ensemble_create(const boids_flock_desc *flocks, uint32_t count, boids_
     ALLOC(&b.bsum, b.nscan_blocks);
     ALLOC(&b.ticket, 1);
     ALLOC(&b.dense_list, boidsgpu::dense_list_capacity(b.ncell, e->total_boids));
-    ALLOC(&b.dense_n, 2);
+    ALLOC(&b.dense_n, 3);
     ALLOC(&b.dflag, b.ncell / 4);
     {
         unsigned char *carry = nullptr;
@@ -293,7 +293,7 @@ int boids_ensemble_create(const boids_flock_desc *flocks, uint32_t count, boids_
     for (uint32_t f = 0; f < count; ++f) link[f] = (float)flocks[f].params.cohesion_sight_distance;
     auto ck = [&](cudaError_t x, const char *w) { return x == cudaSuccess ? 0 : cuda_fail(x, w); };
     if ((rc = ck(cudaMemsetAsync(b.ticket, 0, 4, e->stream), "cudaMemsetAsync")) ||
-        (rc = ck(cudaMemsetAsync(b.dense_n, 0, 8, e->stream), "cudaMemsetAsync")) ||
+        (rc = ck(cudaMemsetAsync(b.dense_n, 0, 12, e->stream), "cudaMemsetAsync")) ||
         (rc = ck(cudaMemcpyAsync(e->d_blk, e->blk_flock.data(), 2 * e->blk_flock.size(), cudaMemcpyHostToDevice,
                                  e->stream), "cudaMemcpyAsync")) ||
         (rc = ck(cudaMemcpyAsync(e->d_cell4, e->cell4.data(), 4 * (size_t)count, cudaMemcpyHostToDevice, e->stream),

@@ -302,6 +302,7 @@ struct GridOut {
     int32_t *dcnt;
     uint64_t *dhash;
     Acc *carry;  // per slot: partial sums of huge cells between id windows (null: no windows)
+    uint32_t *defer, *defer_n;  // k_grid_sparse's deferred boids: (slot, lo_id) pairs and their count (null: none)
 };
 
 template <bool DIAG>
@@ -609,7 +610,7 @@ __global__ void k_grid_classify(const uint32_t *__restrict__ count, const uint32
 // accumulation is always in ascending id.  The per-boid tables (segments, hit
 // buffer, sorted list) live in shared memory, one column per thread: as
 // local memory they overflow L1 and every access goes to L2.
-constexpr int kBufA = 12;
+constexpr int kBufA = 13;
 constexpr int kListA = kListCap;
 constexpr int kRT = 128;      // threads of k_grid_sparse
 constexpr int kSegA = 18;     // at most 9 rows x 2 runs (a run split where x wraps)
@@ -629,21 +630,184 @@ struct SparseSmem {
     uint64_t lst[kListA][kRT];   // accepted neighbours, sorted: id << 32 | slot | flags << 29
 };
 
+// The segments of the boid at pi, whose full-size cell is (cy, cz) along y
+// and z, into the thread's columns of sm.seg0/seg1: in each neighbour row,
+// the x cells that a sphere of radius sqrt(trim_r2) around it reaches.
+// Empty runs are not stored.  Returns the number of candidates.
+__device__ __forceinline__ uint32_t sparse_segments(SparseSmem &sm, int t, float3 pi, int cy, int cz,
+                                                    const GridIn &g, const StepConst &k)
+{
+    const int G = k.G, Gx = k.Gx;
+    const float eps = k.side * 1e-5f;
+    int nseg = 0;
+    uint32_t ncand = 0;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        const int dz = r / 3 - 1, dy = r % 3 - 1;
+        const float ddy = dy == 0 ? 0.f : fmaxf(0.f, dy < 0 ? pi.y - (float)cy * k.side - eps
+                                                          : (float)(cy + 1) * k.side - pi.y - eps);
+        const float ddz = dz == 0 ? 0.f : fmaxf(0.f, dz < 0 ? pi.z - (float)cz * k.side - eps
+                                                          : (float)(cz + 1) * k.side - pi.z - eps);
+        const float rem = k.trim_r2 - ddy * ddy - ddz * ddz;
+        if (!(rem > 0.f)) continue;
+        const float rx = sqrtf(rem);
+        const int lo = __float2int_rd((pi.x - rx) * k.inv_subx);
+        const int hi = __float2int_rd((pi.x + rx) * k.inv_subx);
+        int a0 = lo, a1 = hi + 1, c0 = 0, c1 = 0;  // x-cell runs [a0, a1) and [c0, c1)
+        uint32_t ca = 0, cb = 0;  // x shifts of the runs, 2-bit two's complement: 3 = -F, 1 = +F
+        if (lo < 0) { a0 = lo + Gx; a1 = Gx; ca = 3; c1 = min(hi + 1, Gx); }
+        else if (hi >= Gx) { a1 = Gx; c1 = hi + 1 - Gx; cb = 1; }
+        int zz = cz + dz, yy = cy + dy;
+        zz = zz < 0 ? zz + G : (zz >= G ? zz - G : zz);
+        yy = yy < 0 ? yy + G : (yy >= G ? yy - G : yy);
+        const uint32_t rb = k.cell_base + (uint32_t)(zz * G + yy) * (uint32_t)Gx;
+        // y and z shifts of the row, as the x shifts
+        const uint32_t ysh = cy + dy < 0 ? 3u : (cy + dy >= G ? 1u : 0u);
+        const uint32_t w0 = cz + dz < 0 ? 0x80000000u : 0u, w1 = (ysh << 29) | (cz + dz >= G ? 0x80000000u : 0u);
+        if (a1 > a0) {
+            const uint32_t j0 = slot_start(g.lstart, g.bsum, rb + a0, k), j1 = slot_start(g.lstart, g.bsum, rb + a1, k);
+            if (j1 > j0) {
+                sm.seg0[nseg][t] = j0 | (ca << 29) | w0;
+                sm.seg1[nseg][t] = j1 | w1;
+                ncand += j1 - j0;
+                ++nseg;
+            }
+        }
+        if (c1 > c0) {
+            const uint32_t j0 = slot_start(g.lstart, g.bsum, rb + c0, k), j1 = slot_start(g.lstart, g.bsum, rb + c1, k);
+            if (j1 > j0) {
+                sm.seg0[nseg][t] = j0 | (cb << 29) | w0;
+                sm.seg1[nseg][t] = j1 | w1;
+                ncand += j1 - j0;
+                ++nseg;
+            }
+        }
+    }
+    return ncand;
+}
+
+// One pass of a warp (all lanes call it together) over the candidates of its
+// lanes that still need one: the filter, the exact tests of the buffered
+// hits, and the accepted neighbours with ids above lo_id kept sorted in the
+// thread's column of sm.lst, at most kListA.  Those lanes then accumulate
+// their list; a lane that accepted more than the list held keeps need and
+// moves lo_id up to the last id it accumulated.
+template <bool DIAG>
+__device__ __forceinline__ void sparse_pass(SparseSmem &sm, int t, uint32_t s, float3 pi, const Sight &sight,
+                                            float dot_lim, uint32_t nc, bool &need, int64_t &lo_id, Acc &a,
+                                            const GridIn &g, const StepConst &k)
+{
+    const float3 vi = sight.v;
+    const uint32_t mine = need ? nc : 0;
+    const uint32_t max_nc = __reduce_max_sync(0xffffffffu, mine);
+    int m = 0, nb = 0;
+    uint32_t more = 0;  // accepted neighbours with id > lo_id in this pass
+    int qs = -1;
+    uint32_t j = 0, jend = 0;  // global slots [j, jend) of the current segment
+    uint32_t swrap = 0;        // 1 << 31 when the segment crosses a periodic face
+    float qx = 0.f, qy = 0.f, qz = 0.f;
+    // the next segment (none is empty): its slots and the query point
+    auto advance = [&]() {
+        ++qs;
+        const uint32_t w0 = sm.seg0[qs][t], w1 = sm.seg1[qs][t];
+        j = w0 & 0x1fffffffu;
+        jend = w1 & 0x1fffffffu;
+        // the candidate's image is pj + shift: test pj against pi - shift
+        const int vx = (int)(w0 << 1) >> 30, vy = (int)(w1 << 1) >> 30;
+        const int vz = (int)(w1 >> 31) - (int)(w0 >> 31);
+        qx = __fmaf_rn(-__int2float_rn(vx), k.Ff, pi.x);
+        qy = __fmaf_rn(-__int2float_rn(vy), k.Ff, pi.y);
+        qz = __fmaf_rn(-__int2float_rn(vz), k.Ff, pi.z);
+        swrap = ((w0 | w1) & 0xe0000000u) ? 0x80000000u : 0u;
+    };
+    auto filter = [&](float4 pj, float3 q, uint32_t jc, uint32_t wrap) {
+        const float dx = pj.x - q.x, dy = pj.y - q.y, dz = pj.z - q.z;
+        const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+        const float dv = __fmaf_rn(vi.z, dz, __fmaf_rn(vi.y, dy, __fmul_rn(vi.x, dx)));
+        if (d2 < k.filt_r2 && dv >= dot_lim && jc != s) sm.buf[nb++][t] = jc | wrap;
+    };
+    // two candidates per iteration, so that both loads are in flight together;
+    // the buffers are flushed with room for the next two hits
+    for (uint32_t it = 0; it < max_nc; it += 2) {
+        const bool va = it < mine, vb = it + 1 < mine;
+        uint32_t ca = 0, cb = 0, sa = 0, sb = 0;  // candidate slots and their wrap flags
+        float3 qa = make_float3(0.f, 0.f, 0.f), qb = qa;
+        if (va) {
+            if (j == jend) advance();
+            ca = j++;
+            qa = make_float3(qx, qy, qz);
+            sa = swrap;
+        }
+        if (vb) {
+            if (j == jend) advance();
+            cb = j++;
+            qb = make_float3(qx, qy, qz);
+            sb = swrap;
+        }
+        const float4 pa = va ? __ldg(g.pos + ca) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 pb = vb ? __ldg(g.pos + cb) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (va) filter(pa, qa, ca, sa);
+        if (vb) filter(pb, qb, cb, sb);
+        // exact tests of the buffered hits, the whole warp together
+        if (__any_sync(0xffffffffu, nb >= kBufA - 1) || it + 2 >= max_nc) {
+            for (int q = 0; q < nb; ++q) {
+                const uint32_t wb = sm.buf[q][t];
+                const uint32_t jb = wb & 0x7fffffffu;
+                const float4 pj = __ldg(g.pos + jb);
+                const uint32_t idj = __float_as_uint(pj.w);
+                if ((int64_t)idj <= lo_id) continue;
+                // a filter hit from a segment without periodic shift is nearer
+                // than F/2 on every axis: it is its own minimum image
+                const float3 tt = (wb >> 31) ? image3(xyz(pj), pi, k) : xyz(pj);
+                const int f = pair_flags(pi, sight, tt, k);
+                if (!f) continue;
+                ++more;
+                const uint64_t e = ((uint64_t)idj << 32) | (uint64_t)(jb | ((uint32_t)f << 29));
+                int w;
+                if (m < kListA) w = m++;
+                else if (e < sm.lst[kListA - 1][t]) w = kListA - 1;
+                else continue;
+                while (w > 0 && sm.lst[w - 1][t] > e) { sm.lst[w][t] = sm.lst[w - 1][t]; --w; }
+                sm.lst[w][t] = e;
+            }
+            nb = 0;
+        }
+    }
+    if (need) {
+        for (int q = 0; q < m; ++q) {
+            const uint64_t e = sm.lst[q][t];
+            const uint32_t jj = (uint32_t)e & 0x1fffffffu;
+            const int f = (int)(((uint32_t)e) >> 29);
+            const float3 tt = image3(xyz(__ldg(g.pos + jj)), pi, k);
+            const float3 vj = (f & 4) ? xyz(__ldg(g.vel + jj)) : make_float3(0.f, 0.f, 0.f);
+            acc_add<DIAG>(a, pi, tt, vj, f, (uint32_t)(e >> 32));
+        }
+        if (more <= (uint32_t)m) need = false;
+        else lo_id = (int64_t)(sm.lst[m - 1][t] >> 32);
+    }
+}
+
 template <bool DIAG, bool MULTI>
 __global__ void __launch_bounds__(kRT)
 k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
 {
     static_assert(kRT == kSlotAlign, "a CTA serves one flock");
     __shared__ SparseSmem sm;
-    __shared__ StepConst kf;
+    // the flock's constants (an ensemble's CTA serves one flock); one word otherwise
+    __shared__ __align__(8) uint32_t kf_words[MULTI ? sizeof(StepConst) / 4 : 1];
+    StepConst &kf = *reinterpret_cast<StepConst *>(kf_words);
     if (MULTI) load_flock(kf, ft, ft.blk_flock[blockIdx.x]);
     const StepConst &k = MULTI ? kf : kp;
-    const int G = k.G, Gx = k.Gx;
+    const int G = k.G;
     const int t = threadIdx.x;
+    const int lane = t & 31, wid = t >> 5;
+    const unsigned below = (1u << lane) - 1u;
     // This CTA's boids outside dense cells (the others are k_grid_dense's),
     // compacted onto its first threads so that warps run full and the
     // warps left over exit at once.
-    __shared__ uint32_t cslot[kRT];
+    // (cslot[t] is read only by thread t before it first writes its own
+    // buffer column, which cslot shares)
+    uint32_t *cslot = sm.buf[0];
     __shared__ uint32_t wcount[kRT / 32];
     const uint32_t s0 = blockIdx.x * kRT + t;
     bool mine = s0 - k.slot_base < k.n;
@@ -654,7 +818,6 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
         mine = !__ldg(g.dflag + fc);
     }
     const unsigned bal = __ballot_sync(0xffffffffu, mine);
-    const int lane = t & 31, wid = t >> 5;
     if (lane == 0) wcount[wid] = __popc(bal);
     __syncthreads();
     uint32_t before = 0, total = 0;
@@ -663,147 +826,75 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
         if (i < wid) before += wcount[i];
         total += wcount[i];
     }
-    if (mine) cslot[before + __popc(bal & ((1u << lane) - 1u))] = s0;
+    if (mine) cslot[before + __popc(bal & below)] = s0;
     __syncthreads();
-    bool act = (uint32_t)t < total;
+    if ((uint32_t)(wid * 32) >= total) return;  // the whole warp is idle
+    const bool act = (uint32_t)t < total;
     const uint32_t s = act ? cslot[t] : s0;
     const float4 p4 = act ? g.pos[s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 v4 = act ? g.vel[s] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float3 pi = xyz(p4), vi = xyz(v4);
-    const int cx = cell1(pi.x, k), cy = cell1(pi.y, k), cz = cell1(pi.z, k);
-    // x-cell index of row (dy, dz) around this boid, with the periodic wrap
-    auto row_base = [&](int r) {
-        int zz = cz + r / 3 - 1, yy = cy + r % 3 - 1;
-        zz = zz < 0 ? zz + G : (zz >= G ? zz - G : zz);
-        yy = yy < 0 ? yy + G : (yy >= G ? yy - G : yy);
-        return k.cell_base + (uint32_t)(zz * G + yy) * (uint32_t)Gx;
-    };
-    // This boid's segments: in each neighbour row, the x cells that a sphere
-    // of radius sqrt(trim_r2) around it reaches.
-    int nseg = 0;
-    uint32_t ncand = 0;
-    if (act) {
-        const float eps = k.side * 1e-5f;
-#pragma unroll
-        for (int r = 0; r < 9; ++r) {
-            const int dz = r / 3 - 1, dy = r % 3 - 1;
-            const float ddy = dy == 0 ? 0.f : fmaxf(0.f, dy < 0 ? pi.y - (float)cy * k.side - eps
-                                                              : (float)(cy + 1) * k.side - pi.y - eps);
-            const float ddz = dz == 0 ? 0.f : fmaxf(0.f, dz < 0 ? pi.z - (float)cz * k.side - eps
-                                                              : (float)(cz + 1) * k.side - pi.z - eps);
-            const float rem = k.trim_r2 - ddy * ddy - ddz * ddz;
-            if (!(rem > 0.f)) continue;
-            const float rx = sqrtf(rem);
-            const int lo = __float2int_rd((pi.x - rx) * k.inv_subx);
-            const int hi = __float2int_rd((pi.x + rx) * k.inv_subx);
-            int a0 = lo, a1 = hi + 1, c0 = 0, c1 = 0;  // x-cell runs [a0, a1) and [c0, c1)
-            uint32_t ca = 0, cb = 0;  // x shifts of the runs, 2-bit two's complement: 3 = -F, 1 = +F
-            if (lo < 0) { a0 = lo + Gx; a1 = Gx; ca = 3; c1 = min(hi + 1, Gx); }
-            else if (hi >= Gx) { a1 = Gx; c1 = hi + 1 - Gx; cb = 1; }
-            const uint32_t rb = row_base(r);
-            // y and z shifts of the row, as the x shifts
-            const uint32_t ysh = cy + dy < 0 ? 3u : (cy + dy >= G ? 1u : 0u);
-            const uint32_t w0 = cz + dz < 0 ? 0x80000000u : 0u, w1 = (ysh << 29) | (cz + dz >= G ? 0x80000000u : 0u);
-            // empty runs are not stored: a stored segment always has a candidate
-            if (a1 > a0) {
-                const uint32_t j0 = slot_start(g.lstart, g.bsum, rb + a0, k), j1 = slot_start(g.lstart, g.bsum, rb + a1, k);
-                if (j1 > j0) {
-                    sm.seg0[nseg][t] = j0 | (ca << 29) | w0;
-                    sm.seg1[nseg][t] = j1 | w1;
-                    ncand += j1 - j0;
-                    ++nseg;
-                }
-            }
-            if (c1 > c0) {
-                const uint32_t j0 = slot_start(g.lstart, g.bsum, rb + c0, k), j1 = slot_start(g.lstart, g.bsum, rb + c1, k);
-                if (j1 > j0) {
-                    sm.seg0[nseg][t] = j0 | (cb << 29) | w0;
-                    sm.seg1[nseg][t] = j1 | w1;
-                    ncand += j1 - j0;
-                    ++nseg;
-                }
-            }
-        }
-    }
-    const uint32_t nc = act ? ncand : 0;
-    const uint32_t max_nc = __reduce_max_sync(0xffffffffu, nc);
-    if (max_nc == 0) return;  // the whole warp is idle
-
-    const Sight sight = make_sight(vi);
+    const float3 pi = xyz(p4);
+    const uint32_t nc = act ? sparse_segments(sm, t, pi, cell1(pi.y, k), cell1(pi.z, k), g, k) : 0;
+    const Sight sight = make_sight(xyz(v4));
     const float dot_lim = k.cone_pre ? -(sight.nv * k.dot_eps) : -INFINITY;  // cone pre-test
     Acc a;
     acc_zero(a);
     int64_t lo_id = -1;  // ids <= lo_id were accumulated by earlier passes
     bool need = act;
-    while (__any_sync(0xffffffffu, need)) {
-        int m = 0, nb = 0;
-        uint32_t more = 0;  // accepted neighbours with id > lo_id in this pass
-        int qs = -1;
-        uint32_t j = 0, jend = 0;  // global slots [j, jend) of the current segment
-        uint32_t swrap = 0;        // 1 << 31 when the segment crosses a periodic face
-        float qx = 0.f, qy = 0.f, qz = 0.f;
-        const uint32_t mine = need ? nc : 0;
-        for (uint32_t it = 0; it < max_nc; ++it) {
-            if (it < mine) {
-                if (j == jend) {  // next segment (none is empty)
-                    ++qs;
-                    const uint32_t w0 = sm.seg0[qs][t], w1 = sm.seg1[qs][t];
-                    j = w0 & 0x1fffffffu;
-                    jend = w1 & 0x1fffffffu;
-                    // the candidate's image is pj + shift: test pj against pi - shift
-                    const int vx = (int)(w0 << 1) >> 30, vy = (int)(w1 << 1) >> 30;
-                    const int vz = (int)(w1 >> 31) - (int)(w0 >> 31);
-                    qx = __fmaf_rn(-__int2float_rn(vx), k.Ff, pi.x);
-                    qy = __fmaf_rn(-__int2float_rn(vy), k.Ff, pi.y);
-                    qz = __fmaf_rn(-__int2float_rn(vz), k.Ff, pi.z);
-                    swrap = ((w0 | w1) & 0xe0000000u) ? 0x80000000u : 0u;
-                }
-                const float4 pj = __ldg(g.pos + j);
-                const float dx = pj.x - qx, dy = pj.y - qy, dz = pj.z - qz;
-                const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                const float dv = __fmaf_rn(vi.z, dz, __fmaf_rn(vi.y, dy, __fmul_rn(vi.x, dx)));
-                if (d2 < k.filt_r2 && dv >= dot_lim && j != s) sm.buf[nb++][t] = j | swrap;
-                ++j;
-            }
-            // exact tests of the buffered hits, the whole warp together
-            if (__any_sync(0xffffffffu, nb == kBufA) || it + 1 == max_nc) {
-                for (int q = 0; q < nb; ++q) {
-                    const uint32_t wb = sm.buf[q][t];
-                    const uint32_t jb = wb & 0x7fffffffu;
-                    const float4 pj = __ldg(g.pos + jb);
-                    const uint32_t idj = __float_as_uint(pj.w);
-                    if ((int64_t)idj <= lo_id) continue;
-                    // a filter hit from a segment without periodic shift is nearer
-                    // than F/2 on every axis: it is its own minimum image
-                    const float3 tt = (wb >> 31) ? image3(xyz(pj), pi, k) : xyz(pj);
-                    const int f = pair_flags(pi, sight, tt, k);
-                    if (!f) continue;
-                    ++more;
-                    const uint64_t e = ((uint64_t)idj << 32) | (uint64_t)(jb | ((uint32_t)f << 29));
-                    int w;
-                    if (m < kListA) w = m++;
-                    else if (e < sm.lst[kListA - 1][t]) w = kListA - 1;
-                    else continue;
-                    while (w > 0 && sm.lst[w - 1][t] > e) { sm.lst[w][t] = sm.lst[w - 1][t]; --w; }
-                    sm.lst[w][t] = e;
-                }
-                nb = 0;
-            }
-        }
+    sparse_pass<DIAG>(sm, t, s, pi, sight, dot_lim, nc, need, lo_id, a, g, k);
+    if (!MULTI && o.defer) {
+        // Boids with more accepted neighbours than one list holds go to
+        // k_grid_sparse_more with their partial sums: every further pass
+        // walks all of a lane's candidates, however few lanes of the warp
+        // still need one, and there they run in full warps.
+        const unsigned nbal = __ballot_sync(0xffffffffu, need);
+        uint32_t q0 = 0;
+        if (lane == 0 && nbal) q0 = atomicAdd(o.defer_n, (uint32_t)__popc(nbal));
+        q0 = __shfl_sync(0xffffffffu, q0, 0);
         if (need) {
-            for (int q = 0; q < m; ++q) {
-                const uint64_t e = sm.lst[q][t];
-                const uint32_t jj = (uint32_t)e & 0x1fffffffu;
-                const int f = (int)(((uint32_t)e) >> 29);
-                const float3 tt = image3(xyz(__ldg(g.pos + jj)), pi, k);
-                const float3 vj = (f & 4) ? xyz(__ldg(g.vel + jj)) : make_float3(0.f, 0.f, 0.f);
-                acc_add<DIAG>(a, pi, tt, vj, f, (uint32_t)(e >> 32));
-            }
-            if (more <= (uint32_t)m) need = false;
-            else lo_id = (int64_t)(sm.lst[m - 1][t] >> 32);
+            const uint32_t q = q0 + __popc(nbal & below);
+            o.defer[2 * q] = s;
+            o.defer[2 * q + 1] = (uint32_t)lo_id;
+            o.carry[s] = a;
+        } else if (act) {
+            finish_boid<DIAG>(a, p4, sight.v, s, o, k);
         }
+        return;
     }
-    if (act) finish_boid<DIAG>(a, p4, vi, s, o, k);
+    while (__any_sync(0xffffffffu, need))
+        sparse_pass<DIAG>(sm, t, s, pi, sight, dot_lim, nc, need, lo_id, a, g, k);
+    if (act) finish_boid<DIAG>(a, p4, sight.v, s, o, k);
+}
+
+// The boids k_grid_sparse deferred (single flock only): thread per queued
+// boid, its segments recomputed, further passes from its partial sums.
+template <bool DIAG>
+__global__ void __launch_bounds__(kRT)
+k_grid_sparse_more(GridIn g, GridOut o, StepConst k)
+{
+    __shared__ SparseSmem sm;
+    const int t = threadIdx.x;
+    const uint32_t count = *o.defer_n;
+    for (uint32_t base = blockIdx.x * kRT; base < count; base += gridDim.x * kRT) {
+        if (base + (uint32_t)(t & ~31) >= count) break;  // the whole warp is idle
+        const uint32_t i = base + t;
+        const bool act = i < count;
+        const uint32_t s = act ? o.defer[2 * i] : 0u;
+        int64_t lo_id = act ? (int64_t)o.defer[2 * i + 1] : -1;
+        Acc a;
+        if (act) a = o.carry[s];
+        else acc_zero(a);
+        const float4 p4 = act ? g.pos[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 v4 = act ? g.vel[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float3 pi = xyz(p4);
+        const uint32_t nc = act ? sparse_segments(sm, t, pi, cell1(pi.y, k), cell1(pi.z, k), g, k) : 0;
+        const Sight sight = make_sight(xyz(v4));
+        const float dot_lim = k.cone_pre ? -(sight.nv * k.dot_eps) : -INFINITY;
+        bool need = act;
+        while (__any_sync(0xffffffffu, need))
+            sparse_pass<DIAG>(sm, t, s, pi, sight, dot_lim, nc, need, lo_id, a, g, k);
+        if (act) finish_boid<DIAG>(a, p4, sight.v, s, o, k);
+    }
 }
 
 // ------------------------------------------------------------------ dense cells: CTA per cell
@@ -820,7 +911,9 @@ __device__ uint64_t *block_radix_sort(uint64_t *a, uint64_t *b, uint32_t *hist, 
 {
     __shared__ uint32_t wsum[NT / 32];
     const int t = threadIdx.x;
-    const int K = (n + NT - 1) / NT;
+    // an odd run length keeps the threads' 64-bit reads a[t * K + i] at most
+    // 2-way bank conflicted
+    const int K = ((n + NT - 1) / NT) | 1;
     const int i0 = min(n, t * K), i1 = min(n, i0 + K);
     for (int bit = lo; bit < lo + nbits; bit += 4) {
 #pragma unroll
@@ -1359,7 +1452,7 @@ cudaError_t launch_grid_keys(const StepConst &k, const float4 *pos, uint32_t *ke
 cudaError_t launch_grid_scan(const StepConst &k, const DevBuffers &b, cudaStream_t st, uint64_t *launches,
                              const FlockTable *ft)
 {
-    cudaError_t e = cudaMemsetAsync(b.dense_n, 0, 2 * sizeof(uint32_t), st);  // count, work queue
+    cudaError_t e = cudaMemsetAsync(b.dense_n, 0, 3 * sizeof(uint32_t), st);  // items, work queue, deferred
     if (e != cudaSuccess) return e;
     k_grid_scan<<<b.nscan_blocks, kScanThreads, 0, st>>>(b.count, b.lstart, b.bsum, b.ticket, b.nscan_blocks);
     const uint32_t nfull = b.ncell / 4;
@@ -1418,6 +1511,18 @@ cudaError_t grid_force(const StepConst &k, const GridIn &g, const GridOut &o, co
     cudaError_t e = dense_smem_opt_in<DIAG, MULTI>();
     if (e != cudaSuccess) return e;
     k_grid_sparse<DIAG, MULTI><<<nsp, kRT, 0, st>>>(g, o, k, ft);
+    const unsigned nmore = min(nsp, 2 * b.dense_grid);
+    if (!MULTI && o.defer && b.aux) {
+        // the deferred boids and the dense cells are disjoint: run them side by side
+        if ((e = cudaEventRecord(b.fork, st)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(b.aux, b.fork, 0)) != cudaSuccess) return e;
+        k_grid_sparse_more<DIAG><<<nmore, kRT, 0, b.aux>>>(g, o, k);
+        if ((e = cudaEventRecord(b.join, b.aux)) != cudaSuccess) return e;
+        k_grid_dense<DIAG, MULTI><<<b.dense_grid, kDT, sizeof(DenseSmem), st>>>(g, o, b.dense_list, b.dense_n, k, ft);
+        if ((e = cudaStreamWaitEvent(st, b.join, 0)) != cudaSuccess) return e;
+        return cudaGetLastError();
+    }
+    if (!MULTI && o.defer) k_grid_sparse_more<DIAG><<<nmore, kRT, 0, st>>>(g, o, k);
     k_grid_dense<DIAG, MULTI><<<b.dense_grid, kDT, sizeof(DenseSmem), st>>>(g, o, b.dense_list, b.dense_n, k, ft);
     return cudaGetLastError();
 }
@@ -1432,6 +1537,10 @@ cudaError_t launch_grid_force(const StepConst &k, const DevBuffers &b, int from,
     GridIn g{b.pos[from], b.vel[from], b.lstart, b.bsum, b.dflag};
     GridOut o{};
     o.carry = static_cast<Acc *>(b.carry);
+    if (!ft && b.defer && b.carry) {
+        o.defer = b.defer;
+        o.defer_n = b.dense_n + 2;
+    }
     if (diag) {
         o.dcnt = b.dcnt;
         o.dhash = b.dhash;
@@ -1448,7 +1557,7 @@ cudaError_t launch_grid_force(const StepConst &k, const DevBuffers &b, int from,
     cudaError_t e;
     if (ft) e = diag ? grid_force<true, true>(k, g, o, b, nsp, *ft, st) : grid_force<false, true>(k, g, o, b, nsp, *ft, st);
     else e = diag ? grid_force<true, false>(k, g, o, b, nsp, none, st) : grid_force<false, false>(k, g, o, b, nsp, none, st);
-    if (e == cudaSuccess) *launches += 2;
+    if (e == cudaSuccess) *launches += o.defer ? 3 : 2;
     return e;
 }
 

@@ -88,9 +88,10 @@ size_t layout(const boidsgpu::StepConst &k, unsigned char *base, boidsgpu::DevBu
     b->bsum = reinterpret_cast<uint32_t *>(take(4 * (size_t)b->nscan_blocks));
     b->ticket = reinterpret_cast<uint32_t *>(take(4));
     b->dense_list = reinterpret_cast<uint32_t *>(take(4 * ndense));
-    b->dense_n = reinterpret_cast<uint32_t *>(take(8));
+    b->dense_n = reinterpret_cast<uint32_t *>(take(12));
     b->dflag = take(b->ncell / 4);
     b->carry = nullptr;  // no id windows: cells over the dense list's capacity stay per-boid
+    b->defer = nullptr;  // and the thread-per-boid kernel takes all of its boids' passes
     return off;
 }
 
