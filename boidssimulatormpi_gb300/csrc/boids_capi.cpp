@@ -411,6 +411,27 @@ int make_constants(const boids_params &p, StepConst &k, bool *ref_ok)
     k.inv_subx = G ? (float)(4.0 * G / p.field_size) : 0.f;
     k.side = G ? (float)(p.field_size / G) : 0.f;
     k.trim_r2 = k.filt_r2 * 1.002f;
+    if (G) {
+        // Error budget of the half-precision filter, in scaled units: with
+        // |coordinates| <= 0.5 each conversion and each difference rounds by
+        // at most 2^-12, so a component of the relative vector is off by
+        // e <= 3 * 2^-12 (pairs within the radius have |d| < 0.34); each of
+        // the three fused steps of |d|^2 and v . d adds 2^-11 relative and
+        // 2^-25 absolute.  hfilt: (rf + sqrt(3) e)^2 (1 + 2^-11)^3 + 1e-7.
+        // v . d: 3 * 2^-11 * 0.35 from the velocity's own conversion, plus
+        // |v| (sqrt(3) e + 3 sqrt(3) 2^-11 0.35) + 1e-7 <= 5.2e-4 + 2.2e-3 |v|;
+        // hdot0 and hdot1 take twice that.
+        const double side = p.field_size / G;
+        k.hsc = (float)std::ldexp(1.0, (int)std::floor(std::log2(0.5 / (1.5 * side))));
+        const double vm = k.vmax_f > 0.f ? (double)k.vmax_f : 1.0;
+        k.hvsc = (float)std::ldexp(1.0, (int)std::floor(std::log2(0.5 / vm)));
+        const double e = 3.0 * std::ldexp(1.0, -12);
+        const double r = rf * k.hsc + std::sqrt(3.0) * e;
+        const double hf = r * r * std::pow(1.0 + std::ldexp(1.0, -11), 3) + 1e-7;
+        k.hfilt = std::nextafter((float)hf, INFINITY);
+        k.hdot0 = 1.1e-3f;
+        k.hdot1 = 4.4e-3f;
+    }
     k.dense_min = boidsgpu::kDenseMin;
     k.lone_cand = boidsgpu::kLoneCand;
     k.defer_min = boidsgpu::kDeferMin;

@@ -55,6 +55,14 @@ struct StepConst {
     // three rules.  dot_eps bounds the approximation's error per unit |v|.
     float dot_eps;
     int32_t cone_pre;
+    // The dense kernel's half-precision filter (two candidates per
+    // instruction) works on coordinates relative to the cell's centre times
+    // hsc (a power of two putting them within +-0.5) and velocities times
+    // hvsc (a power of two putting |v| <= vmax within 0.5).  hfilt bounds the
+    // half-precision squared distance of any pair within the filter radius;
+    // a pair is dropped behind the boid when its half-precision v . r is
+    // below -(hdot0 + hdot1 |v| hvsc), which bounds that dot product's error.
+    float hsc, hvsc, hfilt, hdot0, hdot1;
     int32_t id_bits;     // bits needed for the largest boid id, rounded up to a multiple of 4
     RuleConst rule[3];   // cohesion, separation, alignment
     // the reference's overlapping grid, for Boid::grid_index parity

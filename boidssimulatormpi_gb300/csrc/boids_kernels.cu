@@ -22,6 +22,7 @@
 // for the next step (cell key + rank from an atomic count).
 #include "boids_engine.h"
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -944,9 +945,9 @@ constexpr int kBufB = 16;                      // filter hits buffered per lane
 // Accepted neighbours the chunk lanes hand to their owners, 16-bit entries
 // (index | flags << 13).  The owners (chunk 0) keep theirs in registers, so
 // the kChunkPool entries are split over the nbr x (L - 1) other lanes:
-// kChunkPool / (nbr (L - 1)) >= 64 each, 128 when two lanes share a boid.
+// kChunkPool / (nbr (L - 1)) >= 48 each, 96 when two lanes share a boid.
 // Entries are interleaved across lanes (entry-major).
-constexpr int kChunkPool = 8192;
+constexpr int kChunkPool = 6144;
 static_assert(kDenseCap <= (1 << 13), "a list entry holds the candidate index in 13 bits");
 constexpr int kDenseKT = kDenseCap / kDT;      // candidates per thread when the list is full
 
@@ -973,7 +974,10 @@ struct DenseSmem {
     uint32_t work, flock;
     uint32_t nw, cut;              // huge cells: window size, histogram cut
     uint32_t wtot[kDT / 32];       // block scan scratch
-    float4 svel[kDenseCap];        // candidates' velocities, id order
+    float svx[kDenseCap], svy[kDenseCap], svz[kDenseCap];  // candidates' velocities, id order
+    // candidates' coordinates relative to the cell centre, scaled by hsc, in
+    // half precision, two candidates per word (one pad entry for odd counts)
+    __half2 hx[kDenseCap / 2 + 1], hy[kDenseCap / 2 + 1], hz[kDenseCap / 2 + 1];
     StepConst kf;  // the current cell's flock (batched ensembles)
 };
 static_assert(kDenseCap <= 2048, "gather index must fit 11 bits");
@@ -1142,6 +1146,8 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                 block_radix_sort<kDT>(sm.u.keys[0], sm.u.keys[1], sm.v.s.hist, (int)nw, 16, k.id_bits);
             // lay the candidates out in id order over the dead sort buffers
             // (thread t takes positions t, t + kDT, ...: no bank conflicts)
+            const float3 cen = make_float3(((float)cx + 0.5f) * k.side, ((float)cy + 0.5f) * k.side,
+                                           ((float)cz + 0.5f) * k.side);
             uint32_t slot_r[kDenseKT], seg_r[kDenseKT];
 #pragma unroll
             for (int i = 0; i < kDenseKT; ++i) {
@@ -1163,8 +1169,20 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                     sm.u.spos[q] = wrapped ? make_float4(p.x + sh[0], p.y + sh[1], p.z + sh[2],
                                                          __uint_as_float(slot_r[i] | 0x80000000u))
                                            : make_float4(p.x, p.y, p.z, __uint_as_float(slot_r[i]));
-                    sm.svel[q] = __ldg(g.vel + slot_r[i]);
+                    const float4 v = __ldg(g.vel + slot_r[i]);
+                    sm.svx[q] = v.x;
+                    sm.svy[q] = v.y;
+                    sm.svz[q] = v.z;
+                    const float4 cq = sm.u.spos[q];
+                    reinterpret_cast<__half *>(sm.hx)[q] = __float2half_rn((cq.x - cen.x) * k.hsc);
+                    reinterpret_cast<__half *>(sm.hy)[q] = __float2half_rn((cq.y - cen.y) * k.hsc);
+                    reinterpret_cast<__half *>(sm.hz)[q] = __float2half_rn((cq.z - cen.z) * k.hsc);
                 }
+            }
+            if (t == 0 && (nw & 1)) {  // pad the last pair with a candidate far out of reach
+                reinterpret_cast<__half *>(sm.hx)[nw] = __float2half_rn(30000.f);
+                reinterpret_cast<__half *>(sm.hy)[nw] = __float2half_rn(30000.f);
+                reinterpret_cast<__half *>(sm.hz)[nw] = __float2half_rn(30000.f);
             }
             __syncthreads();
             const bool first = lo == 0, last = hi >= k.n;
@@ -1173,7 +1191,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
             for (uint32_t r0 = rbeg; r0 < min(b, rbeg + (uint32_t)kDenseRound); r0 += kDT) {
                 const uint32_t nbr = min(b - r0, (uint32_t)kDT);      // boids this round
                 const uint32_t L = (uint32_t)kDT / nbr;               // lanes per boid
-                const uint32_t csz = (nw + L - 1) / L;                // chunk length
+                const uint32_t csz = ((nw + L - 1) / L + 1) & ~1u;    // chunk length (even: whole pairs)
                 const bool act = (uint32_t)t < nbr * L;
                 const uint32_t bi = act ? (uint32_t)t % nbr : 0, l = act ? (uint32_t)t / nbr : 0;
                 const uint32_t k0 = act ? min(nw, l * csz) : 0, k1 = act ? min(nw, k0 + csz) : 0;
@@ -1190,19 +1208,36 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                 else acc_zero(a);
                 int nb = 0, nl = 0;
                 bool ovf = false;
-                const uint32_t len = k1 - k0;
-                const uint32_t maxlen = __reduce_max_sync(0xffffffffu, len);
+                // The filter in half precision, two candidates per instruction:
+                // it keeps every pair within the filter radius and drops only
+                // pairs whose exact v . r is negative (the bounds are in hfilt,
+                // hdot0 and hdot1); the exact tests decide the rest.
+                const __half2 bx = __float2half2_rn((pi.x - cen.x) * k.hsc);
+                const __half2 by = __float2half2_rn((pi.y - cen.y) * k.hsc);
+                const __half2 bz = __float2half2_rn((pi.z - cen.z) * k.hsc);
+                const float vt = sight.nv * k.hvsc;
+                const bool pre = k.cone_pre && vt <= 1.0f;
+                const __half2 hvx = __float2half2_rn(pre ? vi.x * k.hvsc : 0.f);
+                const __half2 hvy = __float2half2_rn(pre ? vi.y * k.hvsc : 0.f);
+                const __half2 hvz = __float2half2_rn(pre ? vi.z * k.hvsc : 0.f);
+                const __half2 hf2 = __half2half2(__float2half_ru(k.hfilt));
+                const __half2 hd2 = __half2half2(pre ? __float2half_rd(-(k.hdot0 + k.hdot1 * vt))
+                                                     : __ushort_as_half((unsigned short)0xfc00u));  // -inf
+                const uint32_t p0 = k0 >> 1, plen = k1 > k0 ? ((k1 + 1) >> 1) - p0 : 0;  // pairs
+                const uint32_t maxlen = __reduce_max_sync(0xffffffffu, plen);
                 for (uint32_t it = 0; it < maxlen; ++it) {
-                    if (it < len) {
-                        const uint32_t q = k0 + it;
-                        const float4 cq = sm.u.spos[q];
-                        const float dx = cq.x - pi.x, dy = cq.y - pi.y, dz = cq.z - pi.z;
-                        const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                        const float dv = __fmaf_rn(vi.z, dz, __fmaf_rn(vi.y, dy, __fmul_rn(vi.x, dx)));
-                        if (d2 < k.filt_r2 && dv >= dot_lim) sm.bufs[nb++ * kDT + t] = (uint16_t)q;
+                    if (it < plen) {
+                        const uint32_t pp = p0 + it;
+                        const __half2 dx = __hsub2(sm.hx[pp], bx), dy = __hsub2(sm.hy[pp], by),
+                                      dz = __hsub2(sm.hz[pp], bz);
+                        const __half2 d2 = __hfma2(dz, dz, __hfma2(dy, dy, __hmul2(dx, dx)));
+                        const __half2 dv = __hfma2(hvz, dz, __hfma2(hvy, dy, __hmul2(hvx, dx)));
+                        const unsigned keep = __hlt2_mask(d2, hf2) & __hge2_mask(dv, hd2);
+                        if (keep & 0xffffu) sm.bufs[nb++ * kDT + t] = (uint16_t)(2 * pp);
+                        if (keep >> 16) sm.bufs[nb++ * kDT + t] = (uint16_t)(2 * pp + 1);
                     }
                     // exact tests of the buffered hits, the whole warp together
-                    if (__any_sync(0xffffffffu, nb == kBufB) || it + 1 == maxlen) {
+                    if (__any_sync(0xffffffffu, nb >= kBufB - 1) || it + 1 == maxlen) {
                         for (int e = 0; e < nb; ++e) {
                             const uint32_t q = sm.bufs[e * kDT + t];
                             const float4 cq = sm.u.spos[q];
@@ -1212,7 +1247,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                             const int f = pair_flags(pi, sight, tt, k);
                             if (!f) continue;
                             if (l == 0) {
-                                const float3 vj = (f & 4) ? xyz(sm.svel[q]) : make_float3(0.f, 0.f, 0.f);
+                                const float3 vj = (f & 4) ? make_float3(sm.svx[q], sm.svy[q], sm.svz[q]) : make_float3(0.f, 0.f, 0.f);
                                 acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
                             } else if ((uint32_t)nl < lcap) {
                                 sm.v.lists[nl++ * lw + (t - nbr)] = (uint16_t)(q | ((uint32_t)f << 13));
@@ -1242,7 +1277,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                                 const float3 tt = cand_image(cq, pi, g.pos, k);
                                 const int f = pair_flags(pi, sight, tt, k);
                                 if (!f) continue;
-                                const float3 vj = (f & 4) ? xyz(sm.svel[q]) : make_float3(0.f, 0.f, 0.f);
+                                const float3 vj = (f & 4) ? make_float3(sm.svx[q], sm.svy[q], sm.svz[q]) : make_float3(0.f, 0.f, 0.f);
                                 acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
                             }
                         } else {
@@ -1253,7 +1288,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                                 const int f = (int)(v >> 13);
                                 const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
                                 const float3 tt = cand_image(cq, pi, g.pos, k);
-                                const float3 vj = (f & 4) ? xyz(sm.svel[v & 0x1fffu]) : make_float3(0.f, 0.f, 0.f);
+                                const float3 vj = (f & 4) ? make_float3(sm.svx[v & 0x1fffu], sm.svy[v & 0x1fffu], sm.svz[v & 0x1fffu]) : make_float3(0.f, 0.f, 0.f);
                                 acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
                             }
                         }
