@@ -14,7 +14,9 @@
 // Grid step = scan of cell counts -> stable-free scatter into cell order ->
 // two rule kernels that split the boids by the occupancy of their cell:
 //   k_grid_sparse  one thread per boid; candidates of the 27 cells around it
-//                  are filtered, exactly tested, and kept sorted by id;
+//                  are filtered, exactly tested, and kept sorted by id; boids
+//                  that need more than one pass are queued for
+//   k_grid_sparse_more, which runs their further passes in full warps beside
 //   k_grid_dense   one CTA per crowded cell; the 27-cell candidates are
 //                  radix-sorted by id once in shared memory and every boid of
 //                  the cell walks them in that order.
