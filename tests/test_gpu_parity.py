@@ -287,6 +287,40 @@ def test_view_cone_pretest_at_right_angles(boids_lib, oracle_mod, tuning):
     assert_bits_equal(sim.forces(), of, "forces")
 
 
+@pytest.mark.parametrize("tuning", [None, (1, 1, 0, 0)], ids=["default", "all_dense"])
+def test_cells_much_larger_than_the_radius(boids_lib, oracle_mod, tuning):
+    """A large field caps the grid at 128 cells per axis, so cells are three
+    times the radius: the half-precision filter's margins are then relatively
+    wider.  A gathered cluster with a quarter of the boids well over vmax
+    (the filter's view-cone pre-test is off for those) and the rest at rest
+    or in motion; one and three updates against the oracle."""
+    O = oracle_mod
+    n, field = 4096, 20.0
+    prm = dict(O.MARUN2019)
+    p = make_params(O, n, field, prm)
+    rng = np.random.default_rng(31)
+    pos = (rng.random((n, 3)) * 0.3 + 9.85).astype(np.float32)
+    pos[: n // 8] = (rng.random((n // 8, 3)) * field).astype(np.float32)
+    vel = (0.003 * rng.standard_normal((n, 3))).astype(np.float32)
+    vel[n // 4: n // 2] *= 20.0
+    vel[-16:] = 0.0
+    sim = make_sim(boids_lib, "grid", n, field, prm)
+    assert sim.grid_info()["dev_cells_per_axis"] == 128
+    if tuning:
+        sim.set_tuning(*tuning)
+    sim.set_state(pos, vel)
+    cnt, hsh = sim.neighbor_sets()
+    ocnt, ohsh = O.neighbor_sets(p, pos.reshape(-1), vel.reshape(-1))
+    assert np.array_equal(cnt, ocnt) and np.array_equal(hsh, ohsh)
+    assert cnt[:, 0].mean() > 20
+    sim.update(3)
+    op, ov, of = _oracle_run(O, p, "allpairs", pos.reshape(-1), vel.reshape(-1), 3)
+    gp, gv = sim.state()
+    assert_bits_equal(gp, op, "positions")
+    assert_bits_equal(gv, ov, "velocities")
+    assert_bits_equal(sim.forces(), of, "forces")
+
+
 def test_all_round_angles_and_test_ini(boids_lib, oracle_mod):
     """Sight angles >= 1 skip the cone test entirely (src/boid.cpp:29-31)."""
     O = oracle_mod
