@@ -103,9 +103,11 @@ __device__ __forceinline__ int pair_flags(float3 pi, const Sight &s, float3 t, c
     // squared norm, (x*x + y*y) + z*z; relativePos = -d has the same one
     const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
     if (!(d2 < k.d2_any)) return 0;
-    const float rx = __fsub_rn(t.x, pi.x), ry = __fsub_rn(t.y, pi.y), rz = __fsub_rn(t.z, pi.z);
+    // v . relativePos with relativePos = t - pi = -d: round-to-nearest is
+    // symmetric under negation, so the reference's ((v.x r.x + v.y r.y) +
+    // v.z r.z) is exactly the negated sum over d
     const float dot =
-        __fadd_rn(__fadd_rn(__fmul_rn(s.v.x, rx), __fmul_rn(s.v.y, ry)), __fmul_rn(s.v.z, rz));
+        -__fadd_rn(__fadd_rn(__fmul_rn(s.v.x, dx), __fmul_rn(s.v.y, dy)), __fmul_rn(s.v.z, dz));
     const float ca = dot * rsqrtf(d2) * s.inv_nv;  // approximate cosine
     bool exact = !(d2 > 1e-30f) || !(fabsf(ca) < 2.0f);  // tiny distance, 0/0, overflow
     int f = 0;
