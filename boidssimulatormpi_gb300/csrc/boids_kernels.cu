@@ -955,6 +955,8 @@ constexpr int kChunkPool = 6144;
 static_assert(kDenseCap <= (1 << 13), "a list entry holds the candidate index in 13 bits");
 constexpr int kDenseKT = kDenseCap / kDT;      // candidates per thread when the list is full
 
+constexpr int kMaxCuts = 32;                   // id windows of a huge cell planned at once
+
 // Shared memory of k_grid_dense.  Regions whose lifetimes do not overlap
 // share storage: the sort keys become the id-ordered candidate array, and the
 // gather slots and radix histogram become the chunk lists.
@@ -977,6 +979,7 @@ struct DenseSmem {
     float seg_s[18][3];
     uint32_t work, flock;
     uint32_t nw, cut;              // huge cells: window size, histogram cut
+    uint32_t wcut[kMaxCuts], nwcut, wbin;  // huge cells: planned window ends (in bins of wbin ids)
     uint32_t wtot[kDT / 32];       // block scan scratch
     float svx[kDenseCap], svy[kDenseCap], svz[kDenseCap];  // candidates' velocities, id order
     // candidates' coordinates relative to the cell centre, scaled by hsc, in
@@ -1049,6 +1052,58 @@ __device__ uint32_t dense_window(DenseSmem &sm, const GridIn &g, int ns, uint32_
     }
 }
 
+// The id windows of a huge cell planned from one histogram of its
+// candidates' ids over [0, nid) (kWinBins bins of wbin ids): window ends are
+// cut greedily where the running count would pass kDenseCap, at most
+// kMaxCuts of them.  Windows beyond the plan, or past a single bin that alone
+// overflows the list, are cut by dense_window instead.  One histogram pass
+// for all windows, where dense_window needs one per window.
+
+__device__ void dense_window_plan(DenseSmem &sm, const GridIn &g, int ns, uint32_t nid)
+{
+    static_assert((kWinBins + 1) * 4 <= sizeof(sm.u), "the prefix counts live in the sort buffers");
+    static_assert(kWinBins % kDT == 0, "bins per thread");
+    constexpr int kPer = kWinBins / kDT;
+    uint32_t *hist = reinterpret_cast<uint32_t *>(&sm.u);
+    const int t = threadIdx.x;
+    const uint32_t w = (nid + kWinBins - 1) / kWinBins;
+    for (int i = t; i <= kWinBins; i += kDT) hist[i] = 0;
+    __syncthreads();
+    for (int sgi = 0; sgi < ns; ++sgi) {
+        const uint32_t j0 = sm.seg_j0[sgi], len = sm.seg_k0[sgi + 1] - sm.seg_k0[sgi];
+        for (uint32_t q = t; q < len; q += kDT) atomicAdd(&hist[__float_as_uint(__ldg(&g.pos[j0 + q].w)) / w], 1u);
+    }
+    __syncthreads();
+    // exclusive prefix: hist[b] = candidates in bins below b, hist[kWinBins] = all
+    uint32_t loc[kPer], sum = 0;
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) { loc[i] = hist[t * kPer + i]; sum += loc[i]; }
+    uint32_t total;
+    uint32_t pre = block_excl_scan<kDT>(sum, sm.wtot, total);
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) { hist[t * kPer + i] = pre; pre += loc[i]; }
+    if (t == kDT - 1) hist[kWinBins] = pre;
+    __syncthreads();
+    if (t == 0) {
+        uint32_t start = 0, nc = 0;
+        while (start < (uint32_t)kWinBins && nc < (uint32_t)kMaxCuts) {
+            const uint32_t target = hist[start] + (uint32_t)kDenseCap;
+            uint32_t lo_b = start, hi_b = kWinBins + 1;  // hist[lo_b] <= target < hist[hi_b]
+            while (hi_b - lo_b > 1) {
+                const uint32_t mid = (lo_b + hi_b) / 2;
+                if (hist[mid] <= target) lo_b = mid; else hi_b = mid;
+            }
+            if (lo_b == start) break;  // bin `start` alone holds more than the list
+            sm.wcut[nc++] = lo_b;
+            start = lo_b;
+        }
+        sm.nwcut = nc;
+        sm.wbin = w;
+    }
+    __syncthreads();
+}
+
 // One CTA takes one work item at a time (dynamic queue): a crowded cell and
 // up to 128 of its boids (a cell with more boids is several items, taken by
 // several CTAs).  The cell's 27-cell candidates are radix-sorted by id once
@@ -1113,11 +1168,14 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
             continue;
         }
 
+        if (huge) dense_window_plan(sm, g, ns, k.n);
         uint32_t lo = 0;  // this window's ids: [lo, hi)
+        uint32_t wi = 0;  // windows done
         for (;;) {
             uint32_t hi = k.n, nw = ncand;
             if (huge) {
-                hi = dense_window(sm, g, ns, lo, k.n);
+                hi = wi < sm.nwcut ? min(k.n, sm.wcut[wi] * sm.wbin) : dense_window(sm, g, ns, lo, k.n);
+                ++wi;
                 // gather the window's (id, segment, gather index) keys
                 if (t == 0) sm.nw = 0;
                 __syncthreads();
