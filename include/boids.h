@@ -13,7 +13,9 @@
  * reference's getters and its .ptcl frames use.  Every call returns
  * BOIDS_OK (0) or a negative status; boids_last_error() gives the message.
  * Nothing calls exit().  A handle is not thread-safe; all of its GPU work is
- * ordered on one CUDA stream.
+ * ordered on one CUDA stream (a grid update forks part of its work onto a
+ * side stream of the handle and joins it back before the update ends, so
+ * work queued after it on the stream sees the finished state).
  */
 #ifndef BOIDS_GB300_H
 #define BOIDS_GB300_H
