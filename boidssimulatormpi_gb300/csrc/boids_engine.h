@@ -127,12 +127,14 @@ struct DevBuffers {
 
 constexpr int kScanTile = 2048;       // cells per scan block (256 threads x 8)
 constexpr int kListCap = 12;          // grid engine, thread-per-boid kernel: sorted neighbours kept per pass
-// Defaults: the lowest thresholds that keep the first tens of steps from a
-// uniform start at full speed (at N = 2^20, lone_cand 64 or dense_min 8
-// cost 25 % to 4x there, as many small cells become CTA work items).
-// Gathered flocks run up to 2x faster with lone_cand 96 than 384 and
-// another 20 % with lower values still, which the autotuners pick.
-constexpr int kDenseMin = 12;         // default dense_min
+// Defaults, measured on the bench workload (N = 2^20 from a uniform start,
+// steps 5-25), the same flock after 1000 steps, and gathered flocks of 16 384
+// and 65 536 boids: dense_min 16 beats 12 on all four (3-6 %); lone_cand 64
+// costs 5x on the uniform start, as many small cells become CTA work items,
+// and lone_cand above 96 costs the small gathered flocks 5-20 %.  Clustered
+// flocks run another 15-40 % faster with lower thresholds still, which the
+// autotuners pick.
+constexpr int kDenseMin = 16;         // default dense_min
 constexpr int kDeferMin = 4;          // default defer_min
 constexpr int kCandDefer = 192;       // default cand_defer
 constexpr int kLoneCand = 96;         // default lone_cand
@@ -143,7 +145,7 @@ constexpr int kCarryBytes = 72;       // partial sums of one boid between id win
 // states favour low thresholds, uniform states high ones.
 constexpr uint32_t kNever = 1u << 30;
 constexpr uint32_t kTuneCand[][4] = {
-    {12, 4, 192, 96}, {12, 4, 192, 384}, {12, 4, 192, 64}, {12, 4, 192, 48},
+    {16, 4, 192, 96}, {12, 4, 192, 96}, {12, 4, 192, 384}, {12, 4, 192, 64}, {12, 4, 192, 48},
     {8, 2, 96, 128}, {4, 2, 64, 128}, {8, 4, 128, 64}, {kNever, kNever, kNever, 1024},
 };
 constexpr int kTuneCount = sizeof(kTuneCand) / sizeof(kTuneCand[0]);

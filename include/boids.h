@@ -166,7 +166,7 @@ int boids_profile_read(boids_sim *sim, boids_profile_t *out, int32_t reset);
  * tune[1] defer_min   ... or this many with over
  * tune[2] cand_defer  candidates in the cell's 27-cell neighbourhood,
  * tune[3] lone_cand   ... or any boid with over this many candidates.
- * Defaults 12, 4, 192, 96.  No counterpart in the reference. */
+ * Defaults 16, 4, 192, 96.  No counterpart in the reference. */
 int boids_set_tuning(boids_sim *sim, const int32_t *tune4);
 int boids_get_tuning(boids_sim *sim, int32_t *tune4);
 
