@@ -609,12 +609,15 @@ __global__ void k_grid_classify(const uint32_t *__restrict__ count, const uint32
 // All lanes of a warp walk their own candidates in lock-step (a flat loop of
 // max-over-warp length).  Candidates passing the squared-distance filter are
 // buffered, and the whole warp runs the exact tests on its buffers together
-// whenever one of them is full, so the expensive test runs with most lanes
-// busy.  Accepted neighbours are kept sorted by id, at most kListA per pass; a
-// boid with more takes further passes, each keeping the next kListA ids, so
-// accumulation is always in ascending id.  The per-boid tables (segments, hit
-// buffer, sorted list) live in shared memory, one column per thread: as
-// local memory they overflow L1 and every access goes to L2.
+// whenever one of them is nearly full, so the expensive test runs with most
+// lanes busy.  The filter drops candidates behind the boid (the view-cone
+// pre-test, StepConst::dot_eps).  Accepted neighbours are kept sorted by id,
+// at most kListA per pass; a boid with more takes further passes, each
+// keeping the next kListA ids, so accumulation is always in ascending id --
+// for a single flock in k_grid_sparse_more, so that those passes run in full
+// warps.  The per-boid tables (segments, hit buffer, sorted list) live in
+// shared memory, one column per thread: as local memory they overflow L1 and
+// every access goes to L2.
 constexpr int kBufA = 13;
 constexpr int kListA = kListCap;
 constexpr int kRT = 128;      // threads of k_grid_sparse
@@ -1108,13 +1111,14 @@ __device__ void dense_window_plan(DenseSmem &sm, const GridIn &g, int ns, uint32
 // up to 128 of its boids (a cell with more boids is several items, taken by
 // several CTAs).  The cell's 27-cell candidates are radix-sorted by id once
 // per item.  The item's b boids x the candidate list is then split over all
-// threads: each boid gets L = 128/b lanes, lane l walks chunk l of the id-ordered list; chunk 0's lane (the
-// owner) accumulates its accepted neighbours at once, the others hand theirs
-// over in id order and the owner folds them in after its own, so the
-// accumulation order stays ascending id.  A chunk lane whose hand-over list
-// overflows leaves its chunk to the owner.  A cell with more than kDenseCap
-// candidates is done in ascending id windows that each fit the list; the
-// owners carry their partial sums from window to window through o.carry.
+// threads: each boid gets L = 128/b lanes, lane l walks chunk l of the
+// id-ordered list with the half-precision filter; chunk 0's lane (the owner)
+// accumulates its accepted neighbours at once, the others hand theirs over
+// in id order and the owner folds them in after its own, so the accumulation
+// order stays ascending id.  A chunk lane whose hand-over list overflows
+// leaves its chunk to the owner.  A cell with more than kDenseCap candidates
+// is done in ascending id windows that each fit the list; the owners carry
+// their partial sums from window to window through o.carry.
 template <bool DIAG, bool MULTI>
 __global__ void __launch_bounds__(kDT, 4)
 k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint32_t *__restrict__ dense_n,
