@@ -91,6 +91,7 @@ SIGNATURES = {
     "boids_ensemble_stats": (C.c_int, [_vp, _vp]),
     "boids_ensemble_autotune": (C.c_int, [_vp, C.c_int32]),
     "boids_ensemble_tuning": (C.c_int, [_vp, _vp]),
+    "boids_ensemble_set_tuning": (C.c_int, [_vp, _vp]),
     "boids_ensemble_synchronize": (C.c_int, [_vp]),
     "boids_ensemble_kernel_launches": (C.c_uint64, [_vp]),
     "boids_mlp_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_int32, C.POINTER(_vp)]),
@@ -373,6 +374,10 @@ class Ensemble:
         t = np.zeros(4, np.int32)
         _check(lib().boids_ensemble_tuning(self.h, _ptr(t)))
         return tuple(int(x) for x in t)
+
+    def set_tuning(self, dense_min, defer_min, cand_defer, lone_cand):
+        t = np.array([min(int(x), 0x7fffffff) for x in (dense_min, defer_min, cand_defer, lone_cand)], np.int32)
+        _check(lib().boids_ensemble_set_tuning(self.h, _ptr(t)))
 
     def kernel_launches(self):
         return int(lib().boids_ensemble_kernel_launches(self.h))

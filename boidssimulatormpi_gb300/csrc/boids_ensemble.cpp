@@ -530,6 +530,17 @@ int boids_ensemble_tuning(boids_ensemble *e, int32_t *out4)
     return BOIDS_OK;
 }
 
+int boids_ensemble_set_tuning(boids_ensemble *e, const int32_t *t)
+{
+    if (!e || !t) return fail(BOIDS_EINVAL, "boids_ensemble_set_tuning: null argument");
+    for (int i = 0; i < 4; ++i)
+        if (t[i] < 0) return fail(BOIDS_EINVAL, "boids_ensemble_set_tuning: negative threshold");
+    int rc = use_device(e);
+    if (rc) return rc;
+    for (int i = 0; i < 4; ++i) e->tune[i] = (uint32_t)t[i];
+    return upload_table(e);
+}
+
 int boids_ensemble_synchronize(boids_ensemble *e)
 {
     if (!e) return fail(BOIDS_EINVAL, "boids_ensemble_synchronize: null handle");

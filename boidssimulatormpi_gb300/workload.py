@@ -10,7 +10,8 @@ srand48(12345), `presteps` untimed updates (the state after them can be
 saved to and reloaded from --state-file, so a profiler can capture only the
 updates of interest), then `steps` updates timed with synchronised wall
 clock.  Ensemble: the batched sweep of boids_ensemble_* (N log-uniform in
-[2^10, 2^16], factors U[0.7, 1.3] on radii, weights and vmax).
+[2^10, 2^16], factors U[0.7, 1.3] on radii, weights and vmax); its states
+after `presteps` can be saved and reloaded the same way.
 """
 from __future__ import annotations
 
@@ -69,8 +70,18 @@ def ensemble(a):
                        a.seed + i))
         total += n
     ens = Ensemble(flocks)
-    ens.init()
-    ens.step(a.presteps)
+    if a.state_file and os.path.exists(a.state_file):
+        d = np.load(a.state_file)
+        for f in range(a.ensemble):
+            ens.set_state(f, d["pos%d" % f], d["vel%d" % f])
+    else:
+        ens.init()
+        ens.step(a.presteps)
+        if a.state_file:
+            st = {}
+            for f in range(a.ensemble):
+                st["pos%d" % f], st["vel%d" % f] = ens.state(f)
+            np.savez(a.state_file, **st)
     ens.synchronize()
     t0 = time.perf_counter()
     ens.step(a.steps)

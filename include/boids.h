@@ -262,6 +262,9 @@ int boids_ensemble_stats(boids_ensemble *ens, double *out);
 int boids_ensemble_autotune(boids_ensemble *ens, int32_t steps_per_trial);
 /* Chosen thresholds: dense_min, defer_min, cand_defer, lone_cand. */
 int boids_ensemble_tuning(boids_ensemble *ens, int32_t *out4);
+/* Set the thresholds of every flock (the meaning of boids_set_tuning);
+ * results do not depend on them.  No counterpart in the reference. */
+int boids_ensemble_set_tuning(boids_ensemble *ens, const int32_t *tune4);
 int boids_ensemble_synchronize(boids_ensemble *ens);
 uint64_t boids_ensemble_kernel_launches(boids_ensemble *ens);
 

@@ -118,6 +118,24 @@ def test_autotune_keeps_results(boids_lib):
     check_same(ens, singles, "stepping with the tuned thresholds")
 
 
+def test_set_tuning_keeps_results(boids_lib):
+    """boids_ensemble_set_tuning from all-dense to all-sparse thresholds: the
+    trajectories stay the single handles' bit for bit."""
+    B = boids_lib
+    ens, singles = make(B, spec_mixed(B, seed=13))
+    ens.set_tuning(1, 1, 0, 0)
+    assert ens.tuning() == (1, 1, 0, 0)
+    ens.step(30)
+    for s in singles:
+        s.update(30)
+    check_same(ens, singles, "all-dense thresholds")
+    ens.set_tuning(1 << 30, 1 << 30, 1 << 30, 1 << 30)
+    ens.step(20)
+    for s in singles:
+        s.update(20)
+    check_same(ens, singles, "all-sparse thresholds")
+
+
 @pytest.mark.slow
 def test_clustered_flocks_match(boids_lib):
     """Long enough for the flocks to gather (dense-cell kernel in use)."""
