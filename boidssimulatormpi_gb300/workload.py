@@ -71,6 +71,7 @@ def ensemble(a):
         total += n
     ens = Ensemble(flocks)
     if a.state_file and os.path.exists(a.state_file):
+        ens.init()  # then replaced flock by flock
         d = np.load(a.state_file)
         for f in range(a.ensemble):
             ens.set_state(f, d["pos%d" % f], d["vel%d" % f])
