@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--field", type=float, default=4.0)
     ap.add_argument("--seed", type=int, default=12345)
     ap.add_argument("--engine", choices=["grid", "allpairs"], default="grid")
+    ap.add_argument("--allpairs-kernels", action="store_true",
+                    help="all-pairs engine: its own N^2 kernels, not the grid kernels it runs by default")
     ap.add_argument("--late-presteps", type=int, default=1000,
                     help="untimed steps before the supplementary clustered-regime timing (0: skip)")
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
@@ -302,7 +304,7 @@ def run_ours(a):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     m = MARUN2019
-    sim = B.BoidSimulation(a.engine, device=local)
+    sim = B.BoidSimulation(a.engine, device=local, allpairs_kernels=a.allpairs_kernels)
     sim.setup(a.n, a.field, *m["sep"], *m["ali"], *m["coh"], m["vmax"], m["vmin"],
               "random_uniform", a.seed + rank)
     # one non-default stream for the engine, the L2 flush and the timing events
@@ -419,7 +421,8 @@ def run_ours(a):
             "warmup": a.warmup, "ms_per_step": total_ms / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
             "config": dict(workload(a), l2="flushed before every timed step (256 MiB write)",
-                           parallelism="replicas" if ws > 1 else "single GPU"),
+                           parallelism="replicas" if ws > 1 else "single GPU",
+                           kernels="all pairs (N^2)" if a.engine == "allpairs" and a.allpairs_kernels else "grid"),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk.summary(), "late_regime": late, "ensemble": ens,
             "step_ms_min_max": [min(step_ms), max(step_ms)]}

@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(PKG_DIR, "libboids_gb300.so")
 ENGINE_ALLPAIRS = 0
 ENGINE_GRID = 1
 FLAG_RECORD_FORCES = 1
+FLAG_ALLPAIRS_KERNELS = 2
 
 ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "EIO", -5: "ESTATE", -6: "ENOTSUP"}
 
@@ -149,13 +150,17 @@ class BoidSimulation:
 
     ``engine`` picks the link-time variant the reference has: "grid"
     (boidsim_grid, src/boid_simulation_grid.cpp) or "allpairs" (boidsim,
-    src/boid_simulation.cpp).
+    src/boid_simulation.cpp).  The all-pairs engine runs the grid kernels
+    where they fit (bit-identical results); ``allpairs_kernels=True`` keeps
+    it on its own N^2 kernels.
     """
 
-    def __init__(self, engine: str = "grid", device: int = 0, record_forces: bool = False):
+    def __init__(self, engine: str = "grid", device: int = 0, record_forces: bool = False,
+                 allpairs_kernels: bool = False):
         self.engine = {"grid": ENGINE_GRID, "allpairs": ENGINE_ALLPAIRS}[engine]
         self.device = device
         self.record_forces = record_forces
+        self.allpairs_kernels = allpairs_kernels
         self.h = None
         self.N = 0
         self._cache = None
@@ -172,7 +177,8 @@ class BoidSimulation:
                    alignment_sight_distance, alignment_sight_angle, alignment_force_coefficient,
                    cohesion_sight_distance, cohesion_sight_angle, cohesion_force_coefficient,
                    velocity_max, velocity_min, self.engine, self.device,
-                   FLAG_RECORD_FORCES if self.record_forces else 0, 0)
+                   (FLAG_RECORD_FORCES if self.record_forces else 0)
+                   | (FLAG_ALLPAIRS_KERNELS if self.allpairs_kernels else 0), 0)
         h = C.c_void_p()
         _check(lib().boids_create(C.byref(p), C.byref(h)))
         self.h = h

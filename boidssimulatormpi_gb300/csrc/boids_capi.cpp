@@ -164,6 +164,7 @@ struct boids_sim {
     int graph_cur = -1;
     StepConst graph_k{};
     uint64_t graph_launches = 0;  // kernel launches per replay
+    int graph_engine = -1;        // the kernels it was captured with
     bool graph_off = false;       // capture failed once on this handle
 };
 
@@ -397,9 +398,14 @@ int make_constants(const boids_params &p, StepConst &k, bool *ref_ok)
     k.refGS = refGS;
     k.refR = refR;
 
-    // device binning grid: cells of side >= 1.01 * filter radius, capped
+    // device binning grid: cells of side >= 1.01 * filter radius, capped.
+    // The all-pairs engine gets one too (same results, see
+    // BOIDS_FLAG_ALLPAIRS_KERNELS) unless its boids could leave the field in
+    // one step.
+    const bool pairs_on_grid = p.engine == BOIDS_ENGINE_ALLPAIRS && !(p.flags & BOIDS_FLAG_ALLPAIRS_KERNELS) &&
+                               std::fmax(p.velocity_max, p.velocity_min) < p.field_size / 2;
     int G = 0;
-    if (p.engine == BOIDS_ENGINE_GRID && rf > 0) {
+    if ((p.engine == BOIDS_ENGINE_GRID || pairs_on_grid) && rf > 0) {
         double g = std::floor(p.field_size / (rf * 1.01));
         const double cap = std::cbrt(std::fmax(2.0 * k.n, 2097152.0));
         if (g > cap) g = std::floor(cap);
@@ -479,7 +485,7 @@ int boids_create(const boids_params *params, boids_sim **out)
     ALLOC(&b.vel[1], n);
     ALLOC(&b.stage, 6 * n);
     ALLOC(&b.flag, 1, true);
-    if (s->engine == 1) {
+    if (G) {
         b.ncell = (uint32_t)(4 * G) * G * G;
         b.ncell_pad = (b.ncell + 1 + boidsgpu::kScanTile - 1) / boidsgpu::kScanTile * boidsgpu::kScanTile;
         b.nscan_blocks = b.ncell_pad / boidsgpu::kScanTile;
@@ -510,7 +516,8 @@ int boids_create(const boids_params *params, boids_sim **out)
         int nsm = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p.device);
         b.dense_grid = (uint32_t)std::max(1, nsm) * 4;
-    } else {
+    }
+    if (p.engine == BOIDS_ENGINE_ALLPAIRS) {  // its own kernels, for states the grid cannot take
         b.ap_cap = boidsgpu::kApCap;
         ALLOC(&b.ap_cnt, n, true);
         ALLOC(&b.ap_list, n * b.ap_cap);
@@ -550,8 +557,10 @@ int boids_set_state(boids_sim *s, const float *pos3n, const float *vel3n)
     int rc = use_device(s);
     if (rc) return rc;
     const uint32_t n = s->k.n;
-    // the grid engine bins positions into cells: they must lie in the field
-    const bool check = s->p.engine == BOIDS_ENGINE_GRID;
+    // the grid kernels bin positions into cells: they must lie in the field
+    // (the grid engine refuses other states; the all-pairs engine takes them
+    // with its own kernels)
+    const bool check = s->k.G != 0;
     float *dpos = s->b.stage, *dvel = s->b.stage + (size_t)3 * n;
     {
         PhaseTimer t(s, 2);
@@ -567,7 +576,9 @@ int boids_set_state(boids_sim *s, const float *pos3n, const float *vel3n)
         uint32_t bad = 0;
         CK(cudaMemcpyAsync(&bad, s->b.flag, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
-        if (bad) return fail(BOIDS_EINVAL, "grid engine: positions must lie in [0, field_size]");
+        if (bad && s->p.engine == BOIDS_ENGINE_GRID)
+            return fail(BOIDS_EINVAL, "grid engine: positions must lie in [0, field_size]");
+        s->engine = bad ? 0 : 1;
     }
     s->cur = 0;
     if (s->engine == 1 && (rc = grid_bin_fresh(s))) return rc;
@@ -639,7 +650,7 @@ int step_once(boids_sim *s, bool rec)
 bool graph_ready(boids_sim *s, bool rec)
 {
     if (s->graph_off || !s->stream) return false;  // the legacy stream cannot be captured
-    if (s->graph && s->graph_stream == s->stream && s->graph_cur == s->cur &&
+    if (s->graph && s->graph_stream == s->stream && s->graph_cur == s->cur && s->graph_engine == s->engine &&
         std::memcmp(&s->graph_k, &s->k, sizeof(StepConst)) == 0)
         return true;
     if (s->graph) {
@@ -676,6 +687,7 @@ bool graph_ready(boids_sim *s, bool rec)
     s->graph_stream = s->stream;
     s->graph_cur = s->cur;
     s->graph_k = s->k;
+    s->graph_engine = s->engine;
     return true;
 }
 

@@ -69,6 +69,7 @@ struct boids_ensemble {
     cudaStream_t stream = nullptr;
     int cur = 0;           // buffer holding the state
     bool binned = false;   // b.pos[cur] is freshly binned (the next step skips the counting sort)
+    bool keys_stale = false;  // set_state changed b.pos[cur]: recompute every key before the next scan
     bool has_state = false;
     cudaGraphExec_t graph = nullptr;
     uint64_t launches = 0;
@@ -116,8 +117,12 @@ int bin_fresh(boids_ensemble *e)
     CK(boidsgpu::launch_grid_keys(e->ks[0], e->b.pos[e->cur], e->b.key, e->b.rank, e->b.count, e->stream,
                                   &e->launches, &e->ft));
     e->binned = false;
+    e->keys_stale = false;
     return 0;
 }
+
+// Keys for the whole ensemble once after any number of set_state calls.
+int ensure_keys(boids_ensemble *e) { return e->keys_stale ? bin_fresh(e) : 0; }
 
 // One update of every flock, the launches of boids_step's grid engine.
 int step_once(boids_ensemble *e)
@@ -372,7 +377,8 @@ int boids_ensemble_set_state(boids_ensemble *e, uint32_t flock, const float *pos
     CK(cudaMemcpyAsync(e->b.vel[e->cur] + k.slot_base, hv.data(), sizeof(float4) * k.n, cudaMemcpyHostToDevice,
                        e->stream));
     e->binned = false;
-    if ((rc = normalize(e)) || (rc = bin_fresh(e))) return rc;
+    if ((rc = normalize(e))) return rc;
+    e->keys_stale = true;  // binned once, at the next step or statistics pass
     CK(cudaStreamSynchronize(e->stream));
     return BOIDS_OK;
 }
@@ -388,7 +394,7 @@ int boids_ensemble_step(boids_ensemble *e, int32_t steps)
         if ((rc = step_once(e))) return rc;
         ++t;
     }
-    if ((rc = normalize(e))) return rc;
+    if ((rc = normalize(e)) || (rc = ensure_keys(e))) return rc;
     const uint64_t per_step = 4;  // scan, scatter, sparse, dense
     if (steps - t >= kGraphSteps) {
         if ((rc = capture_graph(e))) return rc;
@@ -431,7 +437,7 @@ int boids_ensemble_stats(boids_ensemble *e, double *out)
     if (!e->has_state) return fail(BOIDS_ESTATE, "boids_ensemble_stats: no state");
     int rc = use_device(e);
     if (rc) return rc;
-    if ((rc = bin_now(e))) return rc;
+    if ((rc = ensure_keys(e)) || (rc = bin_now(e))) return rc;
     CK(boidsgpu::launch_ensemble_stats(e->b, e->cur, e->ft, e->d_link, e->d_acc, e->d_com, e->d_largest, e->d_err,
                                        e->stream, &e->launches));
     const size_t nf = e->ks.size();

@@ -948,7 +948,7 @@ __device__ uint64_t *block_radix_sort(uint64_t *a, uint64_t *b, uint32_t *hist, 
 }
 
 constexpr int kDT = 128;                       // threads of k_grid_dense
-constexpr int kBufB = 16;                      // filter hits buffered per lane
+constexpr int kBufB = 24;                      // filter hits buffered per lane
 // Accepted neighbours the chunk lanes hand to their owners, 16-bit entries
 // (index | flags << 13).  The owners (chunk 0) keep theirs in registers, so
 // the kChunkPool entries are split over the nbr x (L - 1) other lanes:

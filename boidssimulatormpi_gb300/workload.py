@@ -31,7 +31,7 @@ def single(a):
     m = MARUN2019
     n = a.boids
     F = a.field or (n / 16384.0) ** (1.0 / 3.0)
-    sim = BoidSimulation(a.engine)
+    sim = BoidSimulation(a.engine, allpairs_kernels=a.allpairs_kernels)
     sim.setup(n, F, *m["sep"], *m["ali"], *m["coh"], m["vmax"], m["vmin"], "random_uniform", a.seed)
     if a.tuning:
         sim.set_tuning(*[int(x) for x in a.tuning.split(",")])
@@ -101,6 +101,7 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--seed", type=int, default=12345)
     ap.add_argument("--engine", choices=["grid", "allpairs"], default="grid")
+    ap.add_argument("--allpairs-kernels", action="store_true", help="all-pairs engine on its own N^2 kernels")
     ap.add_argument("--state-file", default="")
     ap.add_argument("--tuning", default="", help="dense_min,defer_min,cand_defer,lone_cand")
     ap.add_argument("--ensemble", type=int, default=0, help="flocks (0: a single flock)")

@@ -40,6 +40,14 @@ extern "C" {
 
 /* Keep get_force()'s per-rule forces of every step (36 bytes per boid). */
 #define BOIDS_FLAG_RECORD_FORCES 1u
+/* BOIDS_ENGINE_ALLPAIRS: test every ordered pair on the GPU (N^2 work).
+ * Without it the all-pairs engine runs the grid kernels whenever the field
+ * holds at least 3 device cells per axis, the state lies in [0, field_size]
+ * and the speed limits are below field_size / 2: every pair within the
+ * sight radii is still found, each with the same image, and neighbours are
+ * summed in the same ascending id order, so the results are bit-identical
+ * (the reference's own test/compare_grid.sh asserts grid == all-pairs). */
+#define BOIDS_FLAG_ALLPAIRS_KERNELS 2u
 
 typedef struct boids_sim boids_sim;
 

@@ -38,7 +38,12 @@ def make_params(oracle, n, field, prm):
 
 
 def make_sim(B, engine, n, field, prm, record_forces=True):
-    s = B.BoidSimulation(engine, record_forces=record_forces)
+    """engine: "grid", "allpairs" (which runs the grid kernels where they
+    fit) or "pairs" (the all-pairs engine on its own N^2 kernels)."""
+    if engine == "pairs":
+        s = B.BoidSimulation("allpairs", record_forces=record_forces, allpairs_kernels=True)
+    else:
+        s = B.BoidSimulation(engine, record_forces=record_forces)
     s.setup(n, field, *prm["sep"], *prm["ali"], *prm["coh"], prm["vmax"], prm["vmin"])
     return s
 

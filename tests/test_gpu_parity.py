@@ -31,13 +31,13 @@ def _oracle_run(O, p, engine, pos, vel, steps):
     return pos, vel, f
 
 
-@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+@pytest.mark.parametrize("engine", ["grid", "allpairs", "pairs"])
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
 def test_trajectory_bit_exact(boids_lib, oracle_mod, engine, case):
     name, n, field, sname, init, steps = case
     O = oracle_mod
     prm = getattr(O, sname)
-    if engine == "allpairs" and n > 4096:
+    if engine != "grid" and n > 4096:  # the oracle tests every pair
         steps = 3
     p = make_params(O, n, field, prm)
     sim = make_sim(boids_lib, engine, n, field, prm)
@@ -56,7 +56,7 @@ def test_trajectory_bit_exact(boids_lib, oracle_mod, engine, case):
     assert_bits_equal(gf, of, "forces of step %d" % steps)
 
 
-@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+@pytest.mark.parametrize("engine", ["grid", "allpairs", "pairs"])
 def test_single_step_forces_from_identical_state(boids_lib, oracle_mod, engine):
     """The same evolved state is fed to both sides; one step's get_force must match."""
     O = oracle_mod
@@ -110,7 +110,7 @@ def test_reference_cells_bit_exact(boids_lib, oracle_mod):
     assert O.grid_geometry(p)[1] == 15
 
 
-@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+@pytest.mark.parametrize("engine", ["grid", "allpairs", "pairs"])
 def test_neighbor_sets_bit_exact(boids_lib, oracle_mod, engine):
     O = oracle_mod
     n, field = 32768, 1.27
@@ -131,7 +131,7 @@ def test_neighbor_sets_bit_exact(boids_lib, oracle_mod, engine):
     assert_bits_equal(sim.state()[0], op, "step after diagnostics")
 
 
-@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+@pytest.mark.parametrize("engine", ["grid", "allpairs", "pairs"])
 def test_dense_cluster_overflow_paths(boids_lib, oracle_mod, engine):
     """Hundreds of neighbours per boid: more than the per-thread list holds
     (grid: several sorted passes; all-pairs: ordered full scan)."""
@@ -204,7 +204,7 @@ def test_huge_cell_window_narrowing(boids_lib, oracle_mod):
     assert_bits_equal(sim.forces(), of, "forces")
 
 
-@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+@pytest.mark.parametrize("engine", ["grid", "allpairs", "pairs"])
 def test_degenerate_pairs(boids_lib, oracle_mod, engine):
     """Coincident boids (distance 0), zero velocities (0/0 in the cone test),
     boids on the periodic faces and at x == field_size exactly."""
@@ -321,6 +321,34 @@ def test_cells_much_larger_than_the_radius(boids_lib, oracle_mod, tuning):
     assert_bits_equal(sim.forces(), of, "forces")
 
 
+def test_allpairs_engine_kernel_choice(boids_lib, oracle_mod):
+    """The all-pairs engine runs the grid kernels for states inside the field
+    and its own N^2 kernels for states outside it (the reference takes
+    those: its minimum image then decides); both match the oracle's
+    all-pairs update bit for bit."""
+    O = oracle_mod
+    n, field = 2000, 1.0
+    prm = dict(O.MARUN2019)
+    p = make_params(O, n, field, prm)
+    rng = np.random.default_rng(41)
+    pos = rng.random((n, 3), dtype=np.float32)
+    vel = (0.004 * rng.standard_normal((n, 3))).astype(np.float32)
+    sim = make_sim(boids_lib, "allpairs", n, field, prm)
+    for outside in (False, True, False):
+        q = pos.copy()
+        if outside:
+            q[:40, 0] += np.float32(field)      # beyond the far face
+            q[40:80, 1] -= np.float32(0.25)     # below zero
+        sim.set_state(q, vel)
+        assert sim.grid_info()["list_capacity"] == (64 if outside else 12)
+        sim.update(3)
+        op, ov, of = _oracle_run(O, p, "allpairs", q.reshape(-1), vel.reshape(-1), 3)
+        gp, gv = sim.state()
+        assert_bits_equal(gp, op, "positions (outside=%s)" % outside)
+        assert_bits_equal(gv, ov, "velocities (outside=%s)" % outside)
+        assert_bits_equal(sim.forces(), of, "forces (outside=%s)" % outside)
+
+
 def test_all_round_angles_and_test_ini(boids_lib, oracle_mod):
     """Sight angles >= 1 skip the cone test entirely (src/boid.cpp:29-31)."""
     O = oracle_mod
@@ -329,7 +357,7 @@ def test_all_round_angles_and_test_ini(boids_lib, oracle_mod):
     n, field = 4096, 0.6
     p = make_params(O, n, field, prm)
     pos, vel = O.init_state(p, "random_uniform", True, 1)
-    for engine in ("grid", "allpairs"):
+    for engine in ("grid", "allpairs", "pairs"):
         sim = make_sim(boids_lib, engine, n, field, prm)
         sim.set_state(pos, vel)
         sim.update(10)
@@ -341,7 +369,7 @@ def test_all_round_angles_and_test_ini(boids_lib, oracle_mod):
 @pytest.mark.parametrize("n", [0, 1, 2, 33])
 def test_tiny_populations(boids_lib, oracle_mod, n):
     O = oracle_mod
-    for engine in ("grid", "allpairs"):
+    for engine in ("grid", "allpairs", "pairs"):
         p = make_params(O, n, 1.0, O.MARUN2019)
         sim = make_sim(boids_lib, engine, n, 1.0, O.MARUN2019)
         sim.init()
@@ -482,7 +510,7 @@ def test_handle_autotune_keeps_the_trajectory(boids_lib, oracle_mod):
     assert_bits_equal(va, vb, "velocities")
 
 
-@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+@pytest.mark.parametrize("engine", ["grid", "allpairs", "pairs"])
 def test_graph_replayed_steps_equal_single_steps(boids_lib, oracle_mod, engine):
     """boids_step(sim, k >= 32) replays captured 16-update graphs; the same
     updates one call at a time give the same bits and the same launch count."""
