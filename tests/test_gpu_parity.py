@@ -419,6 +419,44 @@ def test_fp64_oracle_tolerance(boids_lib, oracle_mod):
         assert np.all(err[s > 0] <= 1e-4 * s[s > 0])
 
 
+def _polarization(vel):
+    v = np.asarray(vel, np.float64).reshape(-1, 3)
+    sp = np.linalg.norm(v, axis=1)
+    return float(np.linalg.norm((v / np.where(sp > 0, sp, 1)[:, None]).sum(0)) / v.shape[0])
+
+
+@pytest.mark.slow
+def test_allpairs_65536_trajectory_and_polarization(boids_lib, oracle_mod):
+    """The all-pairs workload at N=65536, F=1.6 from the reference's
+    (unseeded) all-pairs init: 1000 updates on the grid kernels and on the
+    N^2 kernels give the same bits at every 50th step (so the same
+    polarization history), and the first 200 updates equal the oracle's bit
+    for bit (its grid port, itself equal to its all-pairs update)."""
+    O = oracle_mod
+    n, field = 65536, 1.6
+    prm = O.MARUN2019
+    p = make_params(O, n, field, prm)
+    sims = [make_sim(boids_lib, e, n, field, prm, record_forces=False) for e in ("allpairs", "pairs")]
+    for s in sims:
+        s.init()
+    pos, vel = O.init_state(p, "random_uniform", False, 12345)
+    assert_bits_equal(sims[0].state()[0], pos, "init")
+    port = O.GridPort(p, pos)
+    pol = []
+    for t in range(50, 1001, 50):
+        for s in sims:
+            s.update(50)
+        (pa, va), (pb, vb) = sims[0].state(), sims[1].state()
+        assert_bits_equal(pa, pb, "grid vs N^2 kernels, step %d" % t)
+        assert_bits_equal(va, vb, "grid vs N^2 kernels, step %d" % t)
+        if t <= 200:
+            port.step(pos, vel, 50)
+            assert_bits_equal(pa, pos, "oracle positions, step %d" % t)
+            assert_bits_equal(va, vel, "oracle velocities, step %d" % t)
+        pol.append(_polarization(va))
+    assert pol[-1] > pol[0] > 0.0  # the flock aligns as it gathers
+
+
 # ---------------------------------------------------------------- golden vectors of the reference
 
 import glob as _glob
