@@ -540,6 +540,7 @@ void boids_destroy(boids_sim *s)
     if (!s) return;
     cudaSetDevice(s->p.device);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->b.aux) cudaStreamSynchronize(s->b.aux);
     free_buffers(s->b);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     if (s->frame_dev) cudaFree(s->frame_dev);
