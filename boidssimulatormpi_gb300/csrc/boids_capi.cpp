@@ -180,6 +180,7 @@ void free_buffers(DevBuffers &b)
     if (b.aux) cudaStreamDestroy(b.aux);
     if (b.fork) cudaEventDestroy(b.fork);
     if (b.join) cudaEventDestroy(b.join);
+    if (b.cjoin) cudaEventDestroy(b.cjoin);
     b = DevBuffers{};
 }
 
@@ -507,7 +508,8 @@ int boids_create(const boids_params *params, boids_sim **out)
         ALLOC(&b.defer, 2 * n);
         if (cudaStreamCreateWithFlags(&b.aux, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&b.join, cudaEventDisableTiming) != cudaSuccess) {
+            cudaEventCreateWithFlags(&b.join, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b.cjoin, cudaEventDisableTiming) != cudaSuccess) {
             const cudaError_t ce = cudaGetLastError();
             free_buffers(b);
             delete s;

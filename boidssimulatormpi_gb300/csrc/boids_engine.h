@@ -116,7 +116,7 @@ struct DevBuffers {
     // Side stream on which the deferred boids run beside the dense kernel,
     // forked from and joined back to the engine's stream (null: in order).
     cudaStream_t aux;
-    cudaEvent_t fork, join;
+    cudaEvent_t fork, join, cjoin;  // cjoin: the classification's end (it runs beside the scatter)
     uint8_t *dflag;            // per full-size cell: 1 when the dense kernel takes it
     void *carry;               // per slot, kCarryBytes: partial sums between id windows (null: no windows)
     uint32_t *flag;            // set_state range check (1 word)

@@ -554,19 +554,20 @@ __device__ __forceinline__ bool dense_rule(uint32_t b, uint32_t ncand, const Ste
     return b > 0 && want && (ncand <= (uint32_t)kDenseCap || windows);
 }
 
-// Per full-size cell, after the scan and before the scatter (the counts are
-// still intact): the dense flag the thread-per-boid kernel reads, and the
-// dense kernel's work list.
+// Per full-size cell, after the scan (from the cell starts alone, so that it
+// can run beside the scatter): the dense flag the thread-per-boid kernel
+// reads, and the dense kernel's work list.
 template <bool MULTI>
-__global__ void k_grid_classify(const uint32_t *__restrict__ count, const uint32_t *__restrict__ lstart,
+__global__ void k_grid_classify(const uint32_t *__restrict__ lstart,
                                 const uint32_t *__restrict__ bsum, uint8_t *__restrict__ dflag,
                                 uint32_t *__restrict__ dense_list, uint32_t *__restrict__ dense_n, uint32_t nfull,
                                 int windows, StepConst kp, FlockTable ft)
 {
     const uint32_t cg = blockIdx.x * blockDim.x + threadIdx.x;
     if (cg >= nfull) return;
-    const uint4 c4 = *reinterpret_cast<const uint4 *>(count + 4 * (size_t)cg);
-    const uint32_t b = c4.x + c4.y + c4.z + c4.w;
+    // boids of the cell from the scan (the counts may be zeroed meanwhile by
+    // the scatter, which runs beside this kernel)
+    const uint32_t b = cell_start(lstart, bsum, 4 * cg + 4) - cell_start(lstart, bsum, 4 * cg);
     uint8_t flag = 0;
     if (b > 0) {
         uint32_t f = 0;
@@ -1558,13 +1559,22 @@ cudaError_t launch_grid_scan(const StepConst &k, const DevBuffers &b, cudaStream
     k_grid_scan<<<b.nscan_blocks, kScanThreads, 0, st>>>(b.count, b.lstart, b.bsum, b.ticket, b.nscan_blocks);
     const uint32_t nfull = b.ncell / 4;
     const int windows = b.carry != nullptr;
+    // with a side stream the classification runs beside the scatter, which
+    // the caller queues next; launch_grid_force waits for it
+    cudaStream_t cs = st;
+    if (b.aux) {
+        if ((e = cudaEventRecord(b.fork, st)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(b.aux, b.fork, 0)) != cudaSuccess) return e;
+        cs = b.aux;
+    }
     if (ft)
-        k_grid_classify<true><<<blocks_for(nfull, 256), 256, 0, st>>>(b.count, b.lstart, b.bsum, b.dflag,
+        k_grid_classify<true><<<blocks_for(nfull, 256), 256, 0, cs>>>(b.lstart, b.bsum, b.dflag,
                                                                        b.dense_list, b.dense_n, nfull, windows, k, *ft);
     else
-        k_grid_classify<false><<<blocks_for(nfull, 256), 256, 0, st>>>(b.count, b.lstart, b.bsum, b.dflag,
+        k_grid_classify<false><<<blocks_for(nfull, 256), 256, 0, cs>>>(b.lstart, b.bsum, b.dflag,
                                                                         b.dense_list, b.dense_n, nfull, windows, k,
                                                                         FlockTable{});
+    if (b.aux && (e = cudaEventRecord(b.cjoin, b.aux)) != cudaSuccess) return e;
     *launches += 2;
     return cudaGetLastError();
 }
@@ -1611,6 +1621,7 @@ cudaError_t grid_force(const StepConst &k, const GridIn &g, const GridOut &o, co
 {
     cudaError_t e = dense_smem_opt_in<DIAG, MULTI>();
     if (e != cudaSuccess) return e;
+    if (b.aux && (e = cudaStreamWaitEvent(st, b.cjoin, 0)) != cudaSuccess) return e;  // the classification
     k_grid_sparse<DIAG, MULTI><<<nsp, kRT, 0, st>>>(g, o, k, ft);
     const unsigned nmore = min(nsp, 2 * b.dense_grid);
     if (!MULTI && o.defer && b.aux) {
