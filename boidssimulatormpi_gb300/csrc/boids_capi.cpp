@@ -506,6 +506,7 @@ int boids_create(const boids_params *params, boids_sim **out)
         }
         ALLOC(&b.dense_n, 3, true);
         ALLOC(&b.defer, 2 * n);
+        b.defer_cnt = b.dense_n + 2;
         if (cudaStreamCreateWithFlags(&b.aux, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&b.join, cudaEventDisableTiming) != cudaSuccess ||

@@ -112,7 +112,9 @@ struct DevBuffers {
     uint64_t *dhash;           // 3 per boid (id order)
     uint32_t *dense_list;      // dense kernel work items (cell, first boid), this step (dense_list_capacity words)
     uint32_t *dense_n;         // dense items, the dense kernel's work queue, deferred sparse boids (3 words)
-    uint32_t *defer;           // sparse boids deferred to further passes: (slot, lo_id), 2 words per boid (null: none)
+    uint32_t *defer;           // sparse boids deferred to further passes: (slot, lo_id), 2 words per slot (null: none);
+                               // a flock's entries start at its slot_base
+    uint32_t *defer_cnt;       // deferred boids per flock (a single flock: dense_n + 2)
     // Side stream on which the deferred boids run beside the dense kernel,
     // forked from and joined back to the engine's stream (null: in order).
     cudaStream_t aux;

@@ -72,6 +72,7 @@ struct boids_ensemble {
     bool keys_stale = false;  // set_state changed b.pos[cur]: recompute every key before the next scan
     bool has_state = false;
     cudaGraphExec_t graph = nullptr;
+    uint64_t graph_launches = 0;  // kernel launches per replay
     uint64_t launches = 0;
     uint32_t tune[4] = {boidsgpu::kDenseMin, boidsgpu::kDeferMin, boidsgpu::kCandDefer, boidsgpu::kLoneCand};
 };
@@ -82,11 +83,15 @@ void release(boids_ensemble *e)
 {
     if (e->graph) cudaGraphExecDestroy(e->graph);
     DevBuffers &b = e->b;
+    if (e->stream) cudaStreamSynchronize(e->stream);
     void *ptrs[] = {b.pos[0], b.pos[1], b.vel[0], b.vel[1], b.key, b.rank, b.count, b.lstart, b.bsum, b.ticket,
-                    b.dense_list, b.dense_n, b.dflag, b.carry, e->d_ks, e->d_blk, e->d_cell4, e->d_link, e->d_acc, e->d_com,
-                    e->d_largest, e->d_err};
+                    b.dense_list, b.dense_n, b.dflag, b.carry, b.defer, b.defer_cnt, e->d_ks, e->d_blk, e->d_cell4,
+                    e->d_link, e->d_acc, e->d_com, e->d_largest, e->d_err};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    if (b.aux) cudaStreamDestroy(b.aux);
+    for (cudaEvent_t ev : {b.fork, b.join, b.cjoin})
+        if (ev) cudaEventDestroy(ev);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
 }
@@ -169,6 +174,7 @@ int capture_graph(boids_ensemble *e)
     const uint64_t before = e->launches;
     for (int t = 0; t < kGraphSteps && !rc; ++t) rc = step_once(e);
     cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+    e->graph_launches = e->launches - before;
     e->launches = before;  // counted when replayed
     if (rc) {
         if (g) cudaGraphDestroy(g);
@@ -276,6 +282,8 @@ int boids_ensemble_create(const boids_flock_desc *flocks, uint32_t count, boids_
         ALLOC(&carry, (size_t)boidsgpu::kCarryBytes * ns);
         b.carry = carry;
     }
+    ALLOC(&b.defer, 2 * ns);
+    ALLOC(&b.defer_cnt, count);
     ALLOC(&e->d_ks, count);
     ALLOC(&e->d_blk, e->blk_flock.size());
     ALLOC(&e->d_cell4, count);
@@ -293,6 +301,15 @@ int boids_ensemble_create(const boids_flock_desc *flocks, uint32_t count, boids_
         e->stream = nullptr;
         release(e);
         return cuda_fail(ce, "cudaStreamCreate");
+    }
+    // the side stream of the grid update (classification beside the
+    // scatter, deferred sparse boids beside the dense kernel)
+    if ((ce = cudaStreamCreateWithFlags(&b.aux, cudaStreamNonBlocking)) != cudaSuccess ||
+        (ce = cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (ce = cudaEventCreateWithFlags(&b.join, cudaEventDisableTiming)) != cudaSuccess ||
+        (ce = cudaEventCreateWithFlags(&b.cjoin, cudaEventDisableTiming)) != cudaSuccess) {
+        release(e);
+        return cuda_fail(ce, "cudaStreamCreate (side stream)");
     }
     std::vector<float> link(count);
     for (uint32_t f = 0; f < count; ++f) link[f] = (float)flocks[f].params.cohesion_sight_distance;
@@ -395,12 +412,11 @@ int boids_ensemble_step(boids_ensemble *e, int32_t steps)
         ++t;
     }
     if ((rc = normalize(e)) || (rc = ensure_keys(e))) return rc;
-    const uint64_t per_step = 4;  // scan, scatter, sparse, dense
     if (steps - t >= kGraphSteps) {
         if ((rc = capture_graph(e))) return rc;
         for (; steps - t >= kGraphSteps; t += kGraphSteps) {
             CK(cudaGraphLaunch(e->graph, e->stream));
-            e->launches += per_step * kGraphSteps;
+            e->launches += e->graph_launches;
         }
     }
     for (; t < steps; ++t)

@@ -307,7 +307,8 @@ struct GridOut {
     int32_t *dcnt;
     uint64_t *dhash;
     Acc *carry;  // per slot: partial sums of huge cells between id windows (null: no windows)
-    uint32_t *defer, *defer_n;  // k_grid_sparse's deferred boids: (slot, lo_id) pairs and their count (null: none)
+    uint32_t *defer, *defer_cnt;  // k_grid_sparse's deferred boids: (slot, lo_id) pairs from the flock's slot_base,
+                                  // and their count per flock (null: none)
 };
 
 template <bool DIAG>
@@ -851,17 +852,17 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
     int64_t lo_id = -1;  // ids <= lo_id were accumulated by earlier passes
     bool need = act;
     sparse_pass<DIAG>(sm, t, s, pi, sight, dot_lim, nc, need, lo_id, a, g, k);
-    if (!MULTI && o.defer) {
+    if (o.defer) {
         // Boids with more accepted neighbours than one list holds go to
         // k_grid_sparse_more with their partial sums: every further pass
         // walks all of a lane's candidates, however few lanes of the warp
         // still need one, and there they run in full warps.
         const unsigned nbal = __ballot_sync(0xffffffffu, need);
         uint32_t q0 = 0;
-        if (lane == 0 && nbal) q0 = atomicAdd(o.defer_n, (uint32_t)__popc(nbal));
+        if (lane == 0 && nbal) q0 = atomicAdd(o.defer_cnt + k.flock, (uint32_t)__popc(nbal));
         q0 = __shfl_sync(0xffffffffu, q0, 0);
         if (need) {
-            const uint32_t q = q0 + __popc(nbal & below);
+            const uint32_t q = k.slot_base + q0 + __popc(nbal & below);
             o.defer[2 * q] = s;
             o.defer[2 * q + 1] = (uint32_t)lo_id;
             o.carry[s] = a;
@@ -875,21 +876,41 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
     if (act) finish_boid<DIAG>(a, p4, sight.v, s, o, k);
 }
 
-// The boids k_grid_sparse deferred (single flock only): thread per queued
-// boid, its segments recomputed, further passes from its partial sums.
-template <bool DIAG>
+// The boids k_grid_sparse deferred: thread per queued boid, its segments
+// recomputed, further passes from its partial sums.  A single flock's queue
+// is walked grid-stride; in an ensemble CTA b takes the b-th block of 128
+// entries of its flock's queue (the flock of slot block b), so that a CTA
+// serves one flock.
+template <bool DIAG, bool MULTI>
 __global__ void __launch_bounds__(kRT)
-k_grid_sparse_more(GridIn g, GridOut o, StepConst k)
+k_grid_sparse_more(GridIn g, GridOut o, StepConst kp, FlockTable ft)
 {
     __shared__ SparseSmem sm;
+    __shared__ __align__(8) uint32_t kf_words[MULTI ? sizeof(StepConst) / 4 : 1];
+    StepConst &kf = *reinterpret_cast<StepConst *>(kf_words);
     const int t = threadIdx.x;
-    const uint32_t count = *o.defer_n;
-    for (uint32_t base = blockIdx.x * kRT; base < count; base += gridDim.x * kRT) {
+    uint32_t first = 0, count, stride;  // entries [first + base, first + count), base += stride
+    uint32_t base = blockIdx.x * kRT;
+    if (MULTI) {
+        const uint32_t f = ft.blk_flock[blockIdx.x];
+        const uint32_t sb = __ldg(&ft.ks[f].slot_base);
+        count = o.defer_cnt[f];
+        base = blockIdx.x * kRT - sb;  // this CTA's block of the flock's queue
+        if (base >= count) return;     // uniform over the CTA
+        first = sb;
+        stride = count;                // one block per CTA
+        load_flock(kf, ft, f);
+    } else {
+        count = o.defer_cnt[0];
+        stride = gridDim.x * kRT;
+    }
+    const StepConst &k = MULTI ? kf : kp;
+    for (; base < count; base += stride) {
         if (base + (uint32_t)(t & ~31) >= count) break;  // the whole warp is idle
         const uint32_t i = base + t;
         const bool act = i < count;
-        const uint32_t s = act ? o.defer[2 * i] : 0u;
-        int64_t lo_id = act ? (int64_t)o.defer[2 * i + 1] : -1;
+        const uint32_t s = act ? o.defer[2 * (first + i)] : 0u;
+        int64_t lo_id = act ? (int64_t)o.defer[2 * (first + i) + 1] : -1;
         Acc a;
         if (act) a = o.carry[s];
         else acc_zero(a);
@@ -1556,6 +1577,8 @@ cudaError_t launch_grid_scan(const StepConst &k, const DevBuffers &b, cudaStream
 {
     cudaError_t e = cudaMemsetAsync(b.dense_n, 0, 3 * sizeof(uint32_t), st);  // items, work queue, deferred
     if (e != cudaSuccess) return e;
+    if (ft && b.defer_cnt && (e = cudaMemsetAsync(b.defer_cnt, 0, sizeof(uint32_t) * ft->count, st)) != cudaSuccess)
+        return e;  // an ensemble's per-flock deferred counts
     k_grid_scan<<<b.nscan_blocks, kScanThreads, 0, st>>>(b.count, b.lstart, b.bsum, b.ticket, b.nscan_blocks);
     const uint32_t nfull = b.ncell / 4;
     const int windows = b.carry != nullptr;
@@ -1623,18 +1646,18 @@ cudaError_t grid_force(const StepConst &k, const GridIn &g, const GridOut &o, co
     if (e != cudaSuccess) return e;
     if (b.aux && (e = cudaStreamWaitEvent(st, b.cjoin, 0)) != cudaSuccess) return e;  // the classification
     k_grid_sparse<DIAG, MULTI><<<nsp, kRT, 0, st>>>(g, o, k, ft);
-    const unsigned nmore = min(nsp, 2 * b.dense_grid);
-    if (!MULTI && o.defer && b.aux) {
+    const unsigned nmore = MULTI ? nsp : min(nsp, 2 * b.dense_grid);
+    if (o.defer && b.aux) {
         // the deferred boids and the dense cells are disjoint: run them side by side
         if ((e = cudaEventRecord(b.fork, st)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(b.aux, b.fork, 0)) != cudaSuccess) return e;
-        k_grid_sparse_more<DIAG><<<nmore, kRT, 0, b.aux>>>(g, o, k);
+        k_grid_sparse_more<DIAG, MULTI><<<nmore, kRT, 0, b.aux>>>(g, o, k, ft);
         if ((e = cudaEventRecord(b.join, b.aux)) != cudaSuccess) return e;
         k_grid_dense<DIAG, MULTI><<<b.dense_grid, kDT, sizeof(DenseSmem), st>>>(g, o, b.dense_list, b.dense_n, k, ft);
         if ((e = cudaStreamWaitEvent(st, b.join, 0)) != cudaSuccess) return e;
         return cudaGetLastError();
     }
-    if (!MULTI && o.defer) k_grid_sparse_more<DIAG><<<nmore, kRT, 0, st>>>(g, o, k);
+    if (o.defer) k_grid_sparse_more<DIAG, MULTI><<<nmore, kRT, 0, st>>>(g, o, k, ft);
     k_grid_dense<DIAG, MULTI><<<b.dense_grid, kDT, sizeof(DenseSmem), st>>>(g, o, b.dense_list, b.dense_n, k, ft);
     return cudaGetLastError();
 }
@@ -1649,9 +1672,9 @@ cudaError_t launch_grid_force(const StepConst &k, const DevBuffers &b, int from,
     GridIn g{b.pos[from], b.vel[from], b.lstart, b.bsum, b.dflag};
     GridOut o{};
     o.carry = static_cast<Acc *>(b.carry);
-    if (!ft && b.defer && b.carry) {
+    if (b.defer && b.defer_cnt && b.carry) {
         o.defer = b.defer;
-        o.defer_n = b.dense_n + 2;
+        o.defer_cnt = b.defer_cnt;
     }
     if (diag) {
         o.dcnt = b.dcnt;
