@@ -174,7 +174,7 @@ void free_buffers(DevBuffers &b)
 {
     void *ptrs[] = {b.pos[0], b.pos[1], b.vel[0], b.vel[1], b.key, b.rank, b.count, b.lstart,
                     b.bsum, b.ticket, b.ap_cnt, b.ap_list, b.forces, b.stage, b.cells8, b.dcnt, b.dhash,
-                    b.dense_list, b.dense_n, b.flag, b.dflag, b.carry, b.defer};
+                    b.dense_list, b.dense_n, b.flag, b.dflag, b.carry, b.defer, b.wscratch};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (b.aux) cudaStreamDestroy(b.aux);
@@ -519,6 +519,8 @@ int boids_create(const boids_params *params, boids_sim **out)
         int nsm = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p.device);
         b.dense_grid = (uint32_t)std::max(1, nsm) * 4;
+        b.wcap = (uint32_t)std::min<size_t>(boidsgpu::kWinScratch, std::max<size_t>(n, 1));
+        ALLOC(&b.wscratch, (size_t)b.wcap * b.dense_grid);
     }
     if (p.engine == BOIDS_ENGINE_ALLPAIRS) {  // its own kernels, for states the grid cannot take
         b.ap_cap = boidsgpu::kApCap;

@@ -115,6 +115,8 @@ struct DevBuffers {
     uint32_t *defer;           // sparse boids deferred to further passes: (slot, lo_id), 2 words per slot (null: none);
                                // a flock's entries start at its slot_base
     uint32_t *defer_cnt;       // deferred boids per flock (a single flock: dense_n + 2)
+    uint64_t *wscratch;        // dense kernel: wcap entries per CTA, a huge cell's candidates filed by window
+    uint32_t wcap;             // (null / 0: every window scans the neighbourhood)
     // Side stream on which the deferred boids run beside the dense kernel,
     // forked from and joined back to the engine's stream (null: in order).
     cudaStream_t aux;
@@ -141,6 +143,7 @@ constexpr int kDeferMin = 4;          // default defer_min
 constexpr int kCandDefer = 192;       // default cand_defer
 constexpr int kLoneCand = 96;         // default lone_cand
 constexpr int kCarryBytes = 72;       // partial sums of one boid between id windows
+constexpr uint32_t kWinScratch = 32768;  // most candidates a CTA files by window (32 windows of 1024)
 
 // Dense-cell threshold sets the autotuners try, {dense_min, defer_min,
 // cand_defer, lone_cand}; the first is the default.  Crowded (clustered)

@@ -85,7 +85,8 @@ void release(boids_ensemble *e)
     DevBuffers &b = e->b;
     if (e->stream) cudaStreamSynchronize(e->stream);
     void *ptrs[] = {b.pos[0], b.pos[1], b.vel[0], b.vel[1], b.key, b.rank, b.count, b.lstart, b.bsum, b.ticket,
-                    b.dense_list, b.dense_n, b.dflag, b.carry, b.defer, b.defer_cnt, e->d_ks, e->d_blk, e->d_cell4,
+                    b.dense_list, b.dense_n, b.dflag, b.carry, b.defer, b.defer_cnt, b.wscratch, e->d_ks, e->d_blk,
+                    e->d_cell4,
                     e->d_link, e->d_acc, e->d_com, e->d_largest, e->d_err};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -295,10 +296,16 @@ int boids_ensemble_create(const boids_flock_desc *flocks, uint32_t count, boids_
     ALLOC(&e->d_com, 3 * (size_t)count);
     ALLOC(&e->d_largest, count);
     ALLOC(&e->d_err, 1);
-#undef ALLOC
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, e->device);
     b.dense_grid = (uint32_t)std::max(1, nsm) * 4;
+    {
+        uint32_t nmax = 1;
+        for (const auto &k : e->ks) nmax = std::max(nmax, k.n);
+        b.wcap = std::min(boidsgpu::kWinScratch, nmax);
+        ALLOC(&b.wscratch, (size_t)b.wcap * b.dense_grid);
+    }
+#undef ALLOC
     cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
     if (ce != cudaSuccess) {
         e->stream = nullptr;

@@ -309,6 +309,8 @@ struct GridOut {
     Acc *carry;  // per slot: partial sums of huge cells between id windows (null: no windows)
     uint32_t *defer, *defer_cnt;  // k_grid_sparse's deferred boids: (slot, lo_id) pairs from the flock's slot_base,
                                   // and their count per flock (null: none)
+    uint64_t *wscratch;           // k_grid_dense: wcap entries per CTA for bucketing huge cells' windows (null: none)
+    uint32_t wcap;
 };
 
 template <bool DIAG>
@@ -1005,6 +1007,8 @@ struct DenseSmem {
     uint32_t work, flock;
     uint32_t nw, cut;              // huge cells: window size, histogram cut
     uint32_t wcut[kMaxCuts], nwcut, wbin;  // huge cells: planned window ends (in bins of wbin ids)
+    uint32_t woff[kMaxCuts + 1];           // and, when bucketed, each planned window's first scratch entry
+    uint32_t wbucketed;
     uint32_t wtot[kDT / 32];       // block scan scratch
     float svx[kDenseCap], svy[kDenseCap], svz[kDenseCap];  // candidates' velocities, id order
     // candidates' coordinates relative to the cell centre, scaled by hsc, in
@@ -1082,9 +1086,14 @@ __device__ uint32_t dense_window(DenseSmem &sm, const GridIn &g, int ns, uint32_
 // cut greedily where the running count would pass kDenseCap, at most
 // kMaxCuts of them.  Windows beyond the plan, or past a single bin that alone
 // overflows the list, are cut by dense_window instead.  One histogram pass
-// for all windows, where dense_window needs one per window.
+// for all windows, where dense_window needs one per window.  With a scratch
+// of cap entries (this CTA's) that holds the planned windows, a second pass
+// files the candidates by bin, and each planned window is then read from
+// the scratch instead of scanning the whole neighbourhood again; an entry is
+// id << 34 | segment << 29 | slot.
 
-__device__ void dense_window_plan(DenseSmem &sm, const GridIn &g, int ns, uint32_t nid)
+__device__ void dense_window_plan(DenseSmem &sm, const GridIn &g, int ns, uint32_t nid, uint64_t *scratch,
+                                  uint32_t cap)
 {
     static_assert((kWinBins + 1) * 4 <= sizeof(sm.u), "the prefix counts live in the sort buffers");
     static_assert(kWinBins % kDT == 0, "bins per thread");
@@ -1125,6 +1134,26 @@ __device__ void dense_window_plan(DenseSmem &sm, const GridIn &g, int ns, uint32
         }
         sm.nwcut = nc;
         sm.wbin = w;
+        sm.woff[0] = 0;
+        for (uint32_t c = 0; c < nc; ++c) sm.woff[c + 1] = hist[sm.wcut[c]];
+        // bucket the planned windows' candidates when the scratch holds them
+        sm.wbucketed = nc > 0 && scratch != nullptr && sm.woff[nc] <= cap;
+    }
+    __syncthreads();
+    if (!sm.wbucketed) return;
+    // File every candidate of the planned windows at its bin's next entry
+    // (the prefix counts become running ends): a window is then the
+    // contiguous run woff[c] .. woff[c + 1] of the scratch, in bin order.
+    const uint32_t last_bin = sm.wcut[sm.nwcut - 1];
+    for (int sgi = 0; sgi < ns; ++sgi) {
+        const uint32_t j0 = sm.seg_j0[sgi], len = sm.seg_k0[sgi + 1] - sm.seg_k0[sgi];
+        for (uint32_t q = t; q < len; q += kDT) {
+            const uint32_t slot = j0 + q;
+            const uint32_t id = __float_as_uint(__ldg(&g.pos[slot].w));
+            const uint32_t bin = id / w;
+            if (bin < last_bin)
+                scratch[atomicAdd(&hist[bin], 1u)] = ((uint64_t)id << 34) | ((uint64_t)sgi << 29) | slot;
+        }
     }
     __syncthreads();
 }
@@ -1194,29 +1223,43 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
             continue;
         }
 
-        if (huge) dense_window_plan(sm, g, ns, k.n);
+        if (huge)
+            dense_window_plan(sm, g, ns, k.n, o.wscratch ? o.wscratch + (size_t)blockIdx.x * o.wcap : nullptr,
+                              o.wcap);
         uint32_t lo = 0;  // this window's ids: [lo, hi)
         uint32_t wi = 0;  // windows done
         for (;;) {
             uint32_t hi = k.n, nw = ncand;
             if (huge) {
-                hi = wi < sm.nwcut ? min(k.n, sm.wcut[wi] * sm.wbin) : dense_window(sm, g, ns, lo, k.n);
-                ++wi;
+                const bool planned = wi < sm.nwcut;
+                hi = planned ? min(k.n, sm.wcut[wi] * sm.wbin) : dense_window(sm, g, ns, lo, k.n);
                 // gather the window's (id, segment, gather index) keys
-                if (t == 0) sm.nw = 0;
-                __syncthreads();
-                for (int sgi = 0; sgi < ns; ++sgi) {
-                    const uint32_t j0 = sm.seg_j0[sgi], len = sm.seg_k0[sgi + 1] - sm.seg_k0[sgi];
+                if (planned && sm.wbucketed) {  // its run of the scratch
+                    const uint64_t *run = o.wscratch + (size_t)blockIdx.x * o.wcap + sm.woff[wi];
+                    const uint32_t len = sm.woff[wi + 1] - sm.woff[wi];
                     for (uint32_t q = t; q < len; q += kDT) {
-                        const uint32_t slot = j0 + q;
-                        const uint32_t id = __float_as_uint(__ldg(&g.pos[slot].w));
-                        if (id >= lo && id < hi) {
-                            const uint32_t qq = atomicAdd(&sm.nw, 1u);
-                            sm.v.s.gslot[qq] = slot;
-                            sm.u.keys[0][qq] = ((uint64_t)id << 16) | ((uint32_t)sgi << 11) | qq;
+                        const uint64_t e = __ldcg(run + q);
+                        sm.v.s.gslot[q] = (uint32_t)e & 0x1fffffffu;
+                        sm.u.keys[0][q] = ((e >> 34) << 16) | (((uint32_t)(e >> 29) & 0x1fu) << 11) | q;
+                    }
+                    if (t == 0) sm.nw = len;
+                } else {  // a scan of the whole neighbourhood for the window's ids
+                    if (t == 0) sm.nw = 0;
+                    __syncthreads();
+                    for (int sgi = 0; sgi < ns; ++sgi) {
+                        const uint32_t j0 = sm.seg_j0[sgi], len = sm.seg_k0[sgi + 1] - sm.seg_k0[sgi];
+                        for (uint32_t q = t; q < len; q += kDT) {
+                            const uint32_t slot = j0 + q;
+                            const uint32_t id = __float_as_uint(__ldg(&g.pos[slot].w));
+                            if (id >= lo && id < hi) {
+                                const uint32_t qq = atomicAdd(&sm.nw, 1u);
+                                sm.v.s.gslot[qq] = slot;
+                                sm.u.keys[0][qq] = ((uint64_t)id << 16) | ((uint32_t)sgi << 11) | qq;
+                            }
                         }
                     }
                 }
+                ++wi;
                 __syncthreads();
                 nw = sm.nw;
             } else {
@@ -1672,6 +1715,8 @@ cudaError_t launch_grid_force(const StepConst &k, const DevBuffers &b, int from,
     GridIn g{b.pos[from], b.vel[from], b.lstart, b.bsum, b.dflag};
     GridOut o{};
     o.carry = static_cast<Acc *>(b.carry);
+    o.wscratch = b.carry ? b.wscratch : nullptr;
+    o.wcap = o.wscratch ? b.wcap : 0;
     if (b.defer && b.defer_cnt && b.carry) {
         o.defer = b.defer;
         o.defer_cnt = b.defer_cnt;
