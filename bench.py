@@ -409,9 +409,13 @@ def run_ours(a):
     if os.path.exists(tr):
         try:
             with open(tr) as f:
-                t = json.load(f).get("rules_dram_bytes_per_boid")
+                tj = json.load(f)
+            t = tj.get("rules_dram_bytes_per_boid")
             if t:
                 roofline["traffic"] = t * a.n
+            # the bound that does bind: instruction issue of the top kernel
+            if tj.get("issue"):
+                roofline["issue"] = tj["issue"]
         except (OSError, ValueError):
             pass
     cpu = None
