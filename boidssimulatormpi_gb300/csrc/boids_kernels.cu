@@ -11,8 +11,9 @@
 // (src/boid_simulation.cpp:161, src/boid_simulation_grid.cpp:191), so the
 // results are bit-identical to the reference's, not merely close.
 //
-// Grid step = scan of cell counts -> stable-free scatter into cell order ->
-// two rule kernels that split the boids by the occupancy of their cell:
+// Grid step = scan of cell counts -> the scatter into cell order, beside the
+// classification of every full-size cell -> rule kernels that split the
+// boids by the occupancy of their cell:
 //   k_grid_sparse  one thread per boid; candidates of the 27 cells around it
 //                  are filtered, exactly tested, and kept sorted by id; boids
 //                  that need more than one pass are queued for
