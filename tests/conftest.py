@@ -76,3 +76,17 @@ def cli(boids_lib):
 
 
 DATA = os.path.join(ROOT, "tests", "data")
+
+
+@pytest.fixture(scope="session")
+def capi_caller(boids_lib, tmp_path_factory):
+    """tests/native/capi_caller.c, a plain C99 caller of the C ABI, compiled
+    with warnings as errors against include/boids.h and linked against the
+    in-tree library."""
+    import subprocess
+    from boidssimulatormpi_gb300 import build as bld
+    exe = str(tmp_path_factory.mktemp("capi") / "capi_caller")
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-O2", "-I", bld.INCLUDE,
+                    os.path.join(ROOT, "tests", "native", "capi_caller.c"), "-L", bld.PKG, "-lboids_gb300",
+                    "-Wl,-rpath," + bld.PKG, "-o", exe], check=True)
+    return exe

@@ -91,3 +91,18 @@ def test_noalloc_rejects_before_device_work(boids_lib):
     dummy = C.c_void_p(16)
     assert L.boids_step_noalloc(C.byref(p), dummy, dummy, dummy, dummy, None) == -1
     assert "grid engine" in L.boids_last_error().decode()
+
+
+def test_c_caller_builds_and_reports_errors(capi_caller, tmp_path):
+    """A C99 program using only include/boids.h compiles with -Wall -Wextra
+    -Werror -pedantic and links against the library.  Its usage error needs
+    no device; without a GPU the library's first device call returns a
+    status and a message instead of aborting the caller."""
+    import subprocess
+    r = subprocess.run([capi_caller], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "usage" in r.stderr
+    r = subprocess.run([capi_caller, "64", "1.0", "2", str(tmp_path / "out.bin")],
+                       capture_output=True, text=True, timeout=120)
+    if r.returncode != 0:  # no usable GPU here
+        assert r.returncode == 3, r.stderr
+        assert "boids_create failed (%d)" % -3 in r.stderr, r.stderr

@@ -575,3 +575,31 @@ def test_graph_replayed_steps_equal_single_steps(boids_lib, oracle_mod, engine):
     for _ in range(40):
         b.update(1)
     assert_bits_equal(a.state()[0], b.state()[0], "positions after retuning")
+
+
+@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+def test_c_caller_frames_equal_the_oracle(capi_caller, oracle_mod, tmp_path, engine):
+    """tests/native/capi_caller.c drives the library from C the way the
+    reference's frame loop drives BoidSimulation (src/main.cpp:187-291): the
+    frame of each step's state, double-buffered while the update runs, then
+    the final state and get_force values.  Every frame equals the oracle."""
+    import subprocess
+    O = oracle_mod
+    n, field, steps = 2048, 0.5, 20
+    out = tmp_path / "frames.bin"
+    r = subprocess.run([capi_caller, str(n), str(field), str(steps), str(out), engine],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    data = np.fromfile(out, dtype=np.float32)
+    assert data.size == (steps + 5) * 3 * n
+    frames = data[:steps * 3 * n].reshape(steps, n, 3)
+    tail = data[steps * 3 * n:]
+    p = make_params(O, n, field, O.MARUN2019)
+    pos, vel = O.init_state(p, "random_uniform", True, 12345)
+    grid = O.GridPort(p, pos) if engine == "grid" else None
+    for t in range(steps):
+        assert_bits_equal(frames[t], pos, "frame %d" % t)
+        f = grid.step(pos, vel, 1, forces=True) if grid else O.step_allpairs(p, pos, vel, 1, forces=True)
+    assert_bits_equal(tail[:3 * n], pos, "final positions")
+    assert_bits_equal(tail[3 * n:6 * n], vel, "final velocities")
+    assert_bits_equal(tail[6 * n:], f, "forces of the last update")
