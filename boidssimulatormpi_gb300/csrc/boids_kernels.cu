@@ -627,6 +627,11 @@ constexpr int kBufA = 13;
 constexpr int kListA = kListCap;
 constexpr int kRT = 128;      // threads of k_grid_sparse
 constexpr int kSegA = 18;     // at most 9 rows x 2 runs (a run split where x wraps)
+// Candidates loaded together in the filter loop: 3 keeps the kernel within
+// 80 registers (6 CTAs per SM, as the shared tables allow) and is 1-2 %
+// faster than 2; 4 takes 96 registers, 5 CTAs per SM, and is 6 % slower.
+constexpr int kCandStep = 3;
+static_assert(kBufA > kCandStep, "the hit buffer holds an iteration's hits");
 
 struct GridIn {
     const float4 *__restrict__ pos;
@@ -739,30 +744,33 @@ __device__ __forceinline__ void sparse_pass(SparseSmem &sm, int t, uint32_t s, f
         const float dv = __fmaf_rn(vi.z, dz, __fmaf_rn(vi.y, dy, __fmul_rn(vi.x, dx)));
         if (d2 < k.filt_r2 && dv >= dot_lim && jc != s) sm.buf[nb++][t] = jc | wrap;
     };
-    // two candidates per iteration, so that both loads are in flight together;
-    // the buffers are flushed with room for the next two hits
-    for (uint32_t it = 0; it < max_nc; it += 2) {
-        const bool va = it < mine, vb = it + 1 < mine;
-        uint32_t ca = 0, cb = 0, sa = 0, sb = 0;  // candidate slots and their wrap flags
-        float3 qa = make_float3(0.f, 0.f, 0.f), qb = qa;
-        if (va) {
-            if (j == jend) advance();
-            ca = j++;
-            qa = make_float3(qx, qy, qz);
-            sa = swrap;
+    // kCandStep candidates per iteration, so that their loads are in flight
+    // together; the buffers are flushed with room for the next kCandStep hits
+    for (uint32_t it = 0; it < max_nc; it += kCandStep) {
+        bool vc[kCandStep];
+        uint32_t cc[kCandStep], sc[kCandStep];  // candidate slots and their wrap flags
+        float3 qc[kCandStep];
+        float4 pc[kCandStep];
+#pragma unroll
+        for (int u = 0; u < kCandStep; ++u) {
+            vc[u] = it + u < mine;
+            cc[u] = 0;
+            sc[u] = 0;
+            qc[u] = make_float3(0.f, 0.f, 0.f);
+            if (vc[u]) {
+                if (j == jend) advance();
+                cc[u] = j++;
+                qc[u] = make_float3(qx, qy, qz);
+                sc[u] = swrap;
+            }
         }
-        if (vb) {
-            if (j == jend) advance();
-            cb = j++;
-            qb = make_float3(qx, qy, qz);
-            sb = swrap;
-        }
-        const float4 pa = va ? __ldg(g.pos + ca) : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 pb = vb ? __ldg(g.pos + cb) : make_float4(0.f, 0.f, 0.f, 0.f);
-        if (va) filter(pa, qa, ca, sa);
-        if (vb) filter(pb, qb, cb, sb);
+#pragma unroll
+        for (int u = 0; u < kCandStep; ++u) pc[u] = vc[u] ? __ldg(g.pos + cc[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < kCandStep; ++u)
+            if (vc[u]) filter(pc[u], qc[u], cc[u], sc[u]);
         // exact tests of the buffered hits, the whole warp together
-        if (__any_sync(0xffffffffu, nb >= kBufA - 1) || it + 2 >= max_nc) {
+        if (__any_sync(0xffffffffu, nb > kBufA - kCandStep) || it + kCandStep >= max_nc) {
             for (int q = 0; q < nb; ++q) {
                 const uint32_t wb = sm.buf[q][t];
                 const uint32_t jb = wb & 0x7fffffffu;
