@@ -106,3 +106,35 @@ def test_c_caller_builds_and_reports_errors(capi_caller, tmp_path):
     if r.returncode != 0:  # no usable GPU here
         assert r.returncode == 3, r.stderr
         assert "boids_create failed (%d)" % -3 in r.stderr, r.stderr
+
+
+def test_missing_library_fails_loudly(boids_lib, monkeypatch):
+    """Without the built library the binding raises; there is no fallback."""
+    monkeypatch.setattr(boids_lib, "_lib", None)
+    monkeypatch.setattr(boids_lib, "LIB_PATH", os.path.join(ROOT, "no-such-dir", "libboids_gb300.so"))
+    with pytest.raises(RuntimeError, match="not built"):
+        boids_lib.lib()
+
+
+def test_product_never_uses_the_oracle():
+    """The oracle is test infrastructure: no module or source file of the
+    package imports, includes or loads it."""
+    import ast
+    pkg = os.path.join(ROOT, "boidssimulatormpi_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        if "_build" in dirpath:
+            continue
+        for f in files:
+            path = os.path.join(dirpath, f)
+            if f.endswith(".py"):
+                tree = ast.parse(open(path).read(), path)
+                for node in ast.walk(tree):
+                    if isinstance(node, ast.Import):
+                        names = [a.name for a in node.names]
+                    elif isinstance(node, ast.ImportFrom):
+                        names = [node.module or ""]
+                    else:
+                        continue
+                    assert not any(n.split(".")[0] == "oracle" for n in names), path
+            elif f.endswith((".cu", ".cpp", ".h")):
+                assert "oracle" not in open(path).read(), path
