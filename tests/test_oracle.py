@@ -134,3 +134,67 @@ def test_oracle_matches_reference_engine_live(oracle_mod, engine):
         assert_bits_equal(vel, rv, "velocities")
         assert_bits_equal(f, eng.forces(), "forces")
         eng.close()
+
+
+def _edge_states(O):
+    """(name, n, field, settings, pos, vel, steps) for degenerate inputs."""
+    m = O.MARUN2019
+    allround = dict(m, sep=(0.01, 1.0, 0.002), ali=(0.05, 1.5, 0.06), coh=(0.05, 2.0, 0.008))
+    cases = []
+    for n in (1, 2, 3):
+        # a short file of boids heading along +x, each within the sight of
+        # the ones behind it (the first two closer than the separation radius)
+        pos = np.array([[0.40 + 0.008 * i + 0.01 * (i > 1), 0.50 + 0.002 * i, 0.30] for i in range(n)], np.float32)
+        vel = np.array([[0.003, 0.0005 * i, 0.0002] for i in range(n)], np.float32)
+        cases.append(("n=%d" % n, n, 1.0, m, pos.reshape(-1), vel.reshape(-1), 20))
+    p = make_params(O, 512, 0.5, allround)
+    pos, vel = O.init_state(p, "random_uniform", True, 5)
+    cases.append(("all-round sight", 512, 0.5, allround, pos, vel, 20))
+    # boids on the field's faces: coordinates exactly 0 and exactly F
+    p = make_params(O, 256, 0.5, m)
+    pos, vel = O.init_state(p, "random_uniform", True, 6)
+    pos = pos.reshape(-1, 3)
+    pos[0:16, 0] = 0.0
+    pos[16:32, 1] = np.float32(0.5)
+    pos[32:48] = np.float32(0.5)
+    pos[48:64, 2] = 0.0
+    cases.append(("faces", 256, 0.5, m, pos.reshape(-1), vel, 10))
+    # coincident boids, zero velocities (the view cone's NaN) and speeds
+    # outside [vmin, vmax] (both clamp branches)
+    p = make_params(O, 192, 0.5, m)
+    pos, vel = O.init_state(p, "random_uniform", True, 7)
+    pos, vel = pos.reshape(-1, 3), vel.reshape(-1, 3)
+    pos[1::8] = pos[0::8]
+    vel[2::8] = 0.0
+    vel[3::8] *= np.float32(4.0)
+    vel[4::8] *= np.float32(0.25)
+    cases.append(("coincident, still, fast and slow", 192, 0.5, m, pos.reshape(-1), vel.reshape(-1), 10))
+    return cases
+
+
+@ref
+@pytest.mark.parametrize("engine", ["grid", "allpairs"])
+def test_oracle_matches_reference_engine_on_edge_cases(oracle_mod, engine):
+    """The oracle against the reference's own engine on degenerate inputs:
+    one to three boids, all-round sight (angles >= 1), boids on the faces of
+    the field (x == 0, x == F), coincident boids, boids at rest and speeds
+    outside the limits."""
+    O = oracle_mod
+    if not O.ref_available(engine):
+        pytest.skip("oracle/_ref missing")
+    for name, n, field, prm, pos, vel, steps in _edge_states(O):
+        p = make_params(O, n, field, prm)
+        eng = O.RefEngine(engine, p, "random_uniform", 1)
+        eng.set_state(pos, vel)
+        pos, vel = pos.copy(), vel.copy()
+        eng.update(steps)
+        if engine == "grid":
+            f = O.GridPort(p, pos).step(pos, vel, steps, forces=True)
+            assert np.array_equal(O.ref_cells(p, pos), eng.grid_index()), name
+        else:
+            f = O.step_allpairs(p, pos, vel, steps, forces=True)
+        rp, rv = eng.state()
+        assert_bits_equal(pos, rp, name + ": positions")
+        assert_bits_equal(vel, rv, name + ": velocities")
+        assert_bits_equal(f, eng.forces(), name + ": forces")
+        eng.close()
