@@ -8,16 +8,6 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_latin_hypercube_strata():
-    from boidssimulatormpi_gb300 import sweep as S
-    u = S.latin_hypercube(64, 8, seed=3)
-    assert u.shape == (64, 8) and (u >= 0).all() and (u < 1).all()
-    for j in range(8):
-        assert sorted(np.floor(u[:, j] * 64).astype(int).tolist()) == list(range(64))
-    p = S.to_params(np.zeros((1, 8)))
-    assert np.allclose(p, S.BASE * S.LOW)
-
-
 def test_screened_values_are_simulated_values(boids_lib):
     from boidssimulatormpi_gb300 import sweep as S
     ut = S.latin_hypercube(256, seed=1)
