@@ -12,7 +12,7 @@ statistics after the run.
 * screened sweep: the surrogate network (``boids_mlp_*``, BF16 tensor-core
   MLP trained on simulated points) ranks every point, and only its predicted
   top fraction is simulated, which also gives the values the sweep reports;
-  the plain simulation stays the judge of the surrogate's error.
+  the plain simulation remains the measure of the surrogate's error.
 
 No counterpart in the reference, which runs one flock per process.
 """

@@ -1,6 +1,6 @@
 """Parameter sweeps (boidssimulatormpi_gb300.sweep): the screened sweep's
 values are the plain simulation's values for the points it picks (the
-simulation stays the judge), and the surrogate ranks a smooth statistic
+simulation decides every reported value), and the surrogate ranks a smooth statistic
 (nearest-neighbour distance) well enough to recover most of its top set."""
 import numpy as np
 import pytest
