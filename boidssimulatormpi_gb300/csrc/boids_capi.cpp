@@ -410,6 +410,11 @@ int make_constants(const boids_params &p, StepConst &k, bool *ref_ok)
         double g = std::floor(p.field_size / (rf * 1.01));
         const double cap = std::cbrt(std::fmax(2.0 * k.n, 2097152.0));
         if (g > cap) g = std::floor(cap);
+        // The 4 G^3 cell keys are formed in int arithmetic (cell_key), so
+        // they must stay below 2^31: G <= 812.  With marun2019's radii only
+        // flocks of more than 2^28 boids at under half the reference's density
+        // reach it; the grid's size never changes a result.
+        if (g > boidsgpu::kMaxGridAxis) g = boidsgpu::kMaxGridAxis;
         G = g >= 3 ? (int)g : 0;  // fewer than 3 cells per axis: scan all pairs
     }
     k.G = G;

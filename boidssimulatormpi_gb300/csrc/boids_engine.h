@@ -169,6 +169,7 @@ inline size_t dense_list_capacity(size_t ncell, size_t n)
 constexpr int kDenseCap = 1024;       // candidates of a dense cell held in shared memory
 constexpr int kApCap = 64;            // all-pairs engine: neighbours kept per boid
 constexpr uint32_t kMaxBoids = 1u << 29;  // slot index packs into 29 bits
+constexpr int kMaxGridAxis = 812;          // device cells per axis: 4 G^3 < 2^31
 
 // Launchers.  Each returns the launch's cudaError_t and adds the number of
 // kernels it launched to *launches.
