@@ -46,7 +46,9 @@ extern "C" {
  * and the speed limits are below field_size / 2: every pair within the
  * sight radii is still found, each with the same image, and neighbours are
  * summed in the same ascending id order, so the results are bit-identical
- * (the reference's own test/compare_grid.sh asserts grid == all-pairs). */
+ * (the reference's own test/compare_grid.sh asserts grid == all-pairs).
+ * The N^2 kernels take at most 65535 * 1024 boids (one update would test
+ * 4.5e15 pairs); beyond that boids_step returns BOIDS_ECUDA. */
 #define BOIDS_FLAG_ALLPAIRS_KERNELS 2u
 
 typedef struct boids_sim boids_sim;
