@@ -138,3 +138,18 @@ def test_product_never_uses_the_oracle():
                     assert not any(n.split(".")[0] == "oracle" for n in names), path
             elif f.endswith((".cu", ".cpp", ".h")):
                 assert "oracle" not in open(path).read(), path
+
+
+def test_header_from_cxx(boids_lib, tmp_path):
+    """include/boids.h compiles as C++11 with -Wall -Wextra -Werror -pedantic
+    and its functions link as extern "C"; a bad configuration is refused
+    before any device work."""
+    import subprocess
+    from boidssimulatormpi_gb300 import build as bld
+    exe = str(tmp_path / "capi_cxx_check")
+    subprocess.run(["g++", "-std=c++11", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", bld.INCLUDE,
+                    os.path.join(ROOT, "tests", "native", "capi_cxx_check.cpp"), "-L", bld.PKG, "-lboids_gb300",
+                    "-Wl,-rpath," + bld.PKG, "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("-1 ") and "field_size" in r.stdout
