@@ -1983,7 +1983,7 @@ cudaError_t launch_ensemble_stats(const DevBuffers &b, int from, const FlockTabl
     if ((e = cudaMemsetAsync(err, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
     k_stat_moments<<<nb, kStatThreads, 0, st>>>(b.pos[from], b.vel[from], ft, acc, parent);
     k_stat_com<<<blocks_for(ft.count, 128), 128, 0, st>>>(acc, ft.ks, ft.count, com);
-    GridIn g{b.pos[from], b.vel[from], b.lstart, b.bsum};
+    GridIn g{b.pos[from], b.vel[from], b.lstart, b.bsum, nullptr};  // k_stat_pairs reads no dense flags
     k_stat_pairs<<<nb, kStatThreads, 0, st>>>(g, ft, com, link, acc, parent, err);
     k_stat_roots<<<blocks_for(ft.nslots, 256), 256, 0, st>>>(ft, parent, size, err);
     k_stat_largest<<<blocks_for(ft.nslots, 256), 256, 0, st>>>(ft, parent, size, largest);
