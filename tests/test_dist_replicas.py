@@ -72,3 +72,11 @@ def test_reference_arm_prints_on_rank_zero_only():
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1 and '"impl": "reference"' in lines[0]
+    import json
+    d = json.loads(lines[0])
+    assert d["unit"] == "boid-steps/s" and d["higher_is_better"] is True and d["value"] > 0
+    assert d["n_gpus"] == 2 and d["steps"] == 1 and d["warmup"] == 1
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["n"] == 4096
