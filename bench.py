@@ -20,6 +20,14 @@ Reference arm (--impl reference): the reference's own CPU engine
 it is present, else the oracle's C port of it, on all host cores, same
 workload; each step is one update() of all N boids.
 
+Supplementary objects of our arm's line: `parity` (the GPU's updates from the
+timed state against the CPU baseline's, bit for bit), `trajectory` (the
+workload's whole 1000-update run from its seeded initial state, timed as one
+region, with default thresholds and with one retune), `late_regime` (steps
+after that run, when the flock has gathered), `allpairs` (the all-pairs
+engine's N^2 kernels at N=65536, F=1.6, against the FP32 lane-issue peak) and
+`ensemble` (the 256-flock batched sweep).
+
 Multi-GPU (torchrun, N > 1): independent replicas, one per GPU, each with its
 own seed; value = boid-steps of all ranks / the slowest rank's time.
 """
@@ -59,7 +67,8 @@ def parse():
     ap.add_argument("--allpairs-kernels", action="store_true",
                     help="all-pairs engine: its own N^2 kernels, not the grid kernels it runs by default")
     ap.add_argument("--late-presteps", type=int, default=1000,
-                    help="untimed steps before the supplementary clustered-regime timing (0: skip)")
+                    help="updates of the supplementary whole-trajectory timing, after which the "
+                         "clustered regime is timed (0: skip both)")
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ensemble-flocks", type=int, default=256,
@@ -76,12 +85,17 @@ def metric(a):
 
 
 def workload(a):
+    """The workload's config object, the same from both arms."""
     what = "all-pairs" if a.engine == "allpairs" else "grid"
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
     return {"workload": "boids %s update, N=%d, F=%g, marun2019.ini, random_uniform seed %d"
                         % (what, a.n, a.field, a.seed),
             "n": a.n, "field_size": a.field, "settings": "marun2019.ini", "dt": 1,
             "init": "random_uniform", "seed": a.seed, "engine": a.engine,
-            "state": "timed from the initial state, after the warm-up steps"}
+            "state": "timed from the initial state, after the warm-up steps",
+            "l2": "flushed before every timed step (256 MiB write)",
+            "parallelism": "replicas" if ws > 1 else "single GPU",
+            "kernels": "all pairs (N^2)" if a.engine == "allpairs" and a.allpairs_kernels else "grid"}
 
 
 def dist_setup(a):
@@ -266,8 +280,12 @@ def run_ensemble(a, B, rank, dist):
 
 # ------------------------------------------------------------------ our arm
 
-def cpu_baseline_sample(a, pos, vel):
-    """The oracle port (or the reference engine) timed on this host, a few steps."""
+def cpu_baseline_sample(a, pos, vel, gpu_after=None):
+    """The oracle port (or the reference engine) timed on this host: a few
+    updates of all N boids from the state the timed GPU steps start from, on
+    all cores, then one update on one thread.  With gpu_after = the GPU's
+    state after the same number of updates from that state, the two are
+    compared bit for bit (`parity`)."""
     import numpy as np
     import oracle as O
     O.build()
@@ -275,6 +293,7 @@ def cpu_baseline_sample(a, pos, vel):
                  MARUN2019["vmax"], MARUN2019["vmin"])
     cores = os.cpu_count() or 1
     k = max(1, a.cpu_sample_steps)
+    p0, v0 = pos.copy(), vel.copy()
     pos, vel = pos.copy(), vel.copy()
     if O.ref_available("grid"):
         eng = O.RefEngine("grid", p, "random_uniform", a.seed)
@@ -282,6 +301,7 @@ def cpu_baseline_sample(a, pos, vel):
         t0 = time.perf_counter()
         eng.update(k)
         dt = time.perf_counter() - t0
+        pos, vel = eng.state()
         kind = "reference"
         what = "src/boid_simulation_grid.cpp from its sources"
     else:
@@ -291,8 +311,110 @@ def cpu_baseline_sample(a, pos, vel):
         dt = time.perf_counter() - t0
         kind = "port"
         what = "oracle C port of src/boid_simulation_grid.cpp"
-    return {"value": a.n * k / dt, "unit": UNIT, "cores": cores, "kind": kind,
-            "sample": "%s, %d update() of all N=%d boids from the timed state" % (what, k, a.n)}
+    out = {"value": a.n * k / dt, "unit": UNIT, "cores": cores, "kind": kind,
+           "sample": "%s, %d update() of all N=%d boids from the timed state" % (what, k, a.n)}
+    # one thread, one update, from the same state (the port: the reference's
+    # engine takes its thread count from OpenMP at load time)
+    q, w = p0.copy(), v0.copy()
+    g1 = O.GridPort(p, q)
+    t0 = time.perf_counter()
+    g1.step(q, w, 1, threads=1)
+    dt1 = time.perf_counter() - t0
+    g1.close()
+    out["single_thread"] = {"value": a.n / dt1, "unit": UNIT, "cores": 1, "kind": "port",
+                            "sample": "oracle C port, 1 update() of all N=%d boids on one thread" % a.n}
+    if gpu_after is not None:
+        gp, gv = (np.ascontiguousarray(x, np.float32).reshape(-1) for x in gpu_after)
+        cp_, cv = (np.ascontiguousarray(x, np.float32).reshape(-1) for x in (pos, vel))
+        bad = int(np.count_nonzero(gp.view(np.uint32) != cp_.view(np.uint32))
+                  + np.count_nonzero(gv.view(np.uint32) != cv.view(np.uint32)))
+        out["parity"] = {"result": "bit-exact" if bad == 0 else "MISMATCH", "mismatched_values": bad,
+                         "values": int(gp.size + gv.size), "updates": k, "against": kind,
+                         "what": "positions and velocities after %d updates from the timed state, "
+                                 "GPU vs %s" % (k, what)}
+    return out
+
+
+def fp32_lane_peak(sm_mhz, sms):
+    """FP32 lane-instructions per second the SMs can issue: 128 lanes per SM
+    per clock."""
+    return sms * 128 * sm_mhz * 1e6
+
+
+def run_allpairs(a, B, local, stream, torch):
+    """The all-pairs engine on its own N^2 kernels at N=65536, F=1.6 (the
+    same density), the reference's src/boid_simulation.cpp configuration:
+    device time per update, and the pair filter's FP32 rate against the
+    lane-issue peak at the sampled SM clock (10 FP32 operations per ordered
+    pair)."""
+    n, field = 65536, 1.6
+    m = MARUN2019
+    sim = B.BoidSimulation("allpairs", device=local, allpairs_kernels=True)
+    sim.setup(n, field, *m["sep"], *m["ali"], *m["coh"], m["vmax"], m["vmin"], "random_uniform", a.seed)
+    sim.set_stream(stream.cuda_stream)
+    sim.init()
+    sim.update(3)
+    steps = 60
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(steps):
+            sim.update(1)
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    sim.close()
+    c = clk.summary()
+    props = torch.cuda.get_device_properties(local)
+    mhz = c["sm_mhz"] or 2070.0
+    pairs = float(n) * n
+    achieved = 10 * pairs / (ms / 1e3)
+    peak = fp32_lane_peak(mhz, props.multi_processor_count)
+    return {"n": n, "field_size": field, "kernels": "all pairs (N^2): k_ap_pairs + k_ap_accumulate",
+            "steps": steps, "ms_per_step": ms, "value": n / (ms / 1e3), "unit": UNIT,
+            "roofline": {"bound": "fp32_issue", "achieved": achieved / 1e12, "peak": peak / 1e12,
+                         "unit": "TFLOP/s (FP32 lane operations)", "frac": achieved / peak,
+                         "ops_per_pair": 10, "pairs_per_step": pairs,
+                         "peak_is": "%d SMs x 128 FP32 lanes x %.0f MHz (sampled)"
+                                    % (props.multi_processor_count, mhz)},
+            "clocks": c}
+
+
+def timed(stream, torch, fn):
+    """Device time of fn()'s work on stream (CUDA events) and its wall time."""
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3
+
+
+def run_trajectory(a, sim, stream, torch, steps, tune_at, tuning):
+    """The whole trajectory of the workload: `steps` updates from the seeded
+    initial state, replayed from captured graphs, timed as one region; with
+    tune_at > 0 the dense-cell thresholds are retuned once after tune_at
+    updates (the autotuner's trial steps are inside the timed region)."""
+    sim.set_tuning(*tuning)
+    sim.init()
+
+    def run():
+        if tune_at > 0:
+            sim.update(tune_at)
+            sim.autotune(2)
+            sim.update(steps - tune_at)
+        else:
+            sim.update(steps)
+
+    dev_ms, wall_ms = timed(stream, torch, run)
+    return {"steps": steps, "autotune_at": tune_at if tune_at > 0 else None, "device_ms": dev_ms,
+            "wall_ms": wall_ms, "ms_per_step": dev_ms / steps, "value": a.n * steps / (dev_ms / 1e3),
+            "unit": UNIT, "tuning_after": list(sim.tuning())}
 
 
 def run_ours(a):
@@ -312,6 +434,7 @@ def run_ours(a):
     torch.cuda.set_stream(stream)
     sim.set_stream(stream.cuda_stream)
     sim.init()
+    default_tuning = sim.tuning()
     flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MiB > L2
 
     def barrier():
@@ -362,12 +485,22 @@ def run_ours(a):
            "h2d_bytes_per_step": int(hp.nbytes + hv.nbytes),
            "d2h_bytes_per_step": int(hp.nbytes + hv.nbytes)}
 
-    # ---- supplementary: the clustered regime later in the trajectory
-    late = None
+    # ---- the GPU's updates from the timed state, for the in-bench parity check
+    k_par = max(1, a.cpu_sample_steps)
+    sim.set_state(pos0.reshape(-1), vel0.reshape(-1))
+    sim.update(k_par)
+    gpu_after = sim.state()
+
+    # ---- supplementary: the whole trajectory, and the clustered regime at its end
+    traj = late = None
     if a.late_presteps > 0:
-        sim.set_state(pos0.reshape(-1), vel0.reshape(-1))
+        traj = {"default_tuning": run_trajectory(a, sim, stream, torch, a.late_presteps, 0, default_tuning),
+                "autotuned": run_trajectory(a, sim, stream, torch, a.late_presteps, a.late_presteps // 4,
+                                            default_tuning)}
+        # the state after the whole trajectory with default thresholds
+        sim.set_tuning(*default_tuning)
+        sim.init()
         sim.update(a.late_presteps)
-        default_tuning = sim.tuning()
         tuned = sim.autotune()  # crowded flocks favour other dense-cell thresholds
         barrier()
         ms = []
@@ -380,11 +513,12 @@ def run_ours(a):
             s1.record(stream)
             s1.synchronize()
             ms.append(s0.elapsed_time(s1))
-        late = {"after_steps": a.warmup + a.late_presteps, "ms_per_step": sum(ms) / len(ms),
+        late = {"after_steps": a.late_presteps, "ms_per_step": sum(ms) / len(ms),
                 "value": a.n * len(ms) / (sum(ms) / 1e3), "unit": UNIT,
                 "tuning": list(tuned), "default_tuning": list(default_tuning)}
 
     sim.close()
+    allpairs = run_allpairs(a, B, local, stream, torch) if a.engine == "grid" and a.n == 1 << 20 else None
     ens = run_ensemble(a, B, rank, dist) if a.ensemble_flocks > 0 else None
     if rank != 0:
         return
@@ -420,15 +554,15 @@ def run_ours(a):
             pass
     cpu = None
     if not a.no_cpu_baseline and a.engine == "grid":
-        cpu = cpu_baseline_sample(a, pos0.reshape(-1), vel0.reshape(-1))
+        cpu = cpu_baseline_sample(a, pos0.reshape(-1), vel0.reshape(-1), gpu_after)
     line = {"metric": metric(a), "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": total_ms / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-            "config": dict(workload(a), l2="flushed before every timed step (256 MiB write)",
-                           parallelism="replicas" if ws > 1 else "single GPU",
-                           kernels="all pairs (N^2)" if a.engine == "allpairs" and a.allpairs_kernels else "grid"),
+            "config": workload(a),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk.summary(), "late_regime": late, "ensemble": ens,
+            "clocks": clk.summary(),
+            "parity": (cpu or {}).get("parity"),
+            "trajectory": traj, "late_regime": late, "allpairs": allpairs, "ensemble": ens,
             "step_ms_min_max": [min(step_ms), max(step_ms)]}
     print(json.dumps(line), flush=True)
 

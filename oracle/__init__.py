@@ -18,7 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REF_SRC_DEFAULT = "/root/reference/src"
+BUILD_REF = os.path.join(HERE, "build_ref.sh")
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -51,13 +51,25 @@ def build(quiet: bool = True) -> str:
     return LIB_PATH
 
 
+def ref_root() -> str | None:
+    """The reference checkout: $REF_ROOT, else the default location that the
+    recipe build_ref.sh names.  None when that directory is absent (machines
+    without the reference sources: there the tests that need them skip)."""
+    root = os.environ.get("REF_ROOT")
+    if not root:
+        r = subprocess.run(["bash", BUILD_REF, "--root"], capture_output=True, text=True)
+        root = r.stdout.strip() if r.returncode == 0 else ""
+    return root if root and os.path.isdir(root) else None
+
+
 def build_ref(src_dir: str | None = None) -> bool:
     """Build oracle/_ref from the reference sources if they are present."""
-    src_dir = src_dir or os.environ.get("REF_SRC", REF_SRC_DEFAULT)
-    if not os.path.exists(os.path.join(src_dir, "boid_simulation_grid.cpp")):
+    if not src_dir:
+        root = ref_root()
+        src_dir = os.environ.get("REF_SRC") or (os.path.join(root, "src") if root else "")
+    if not src_dir or not os.path.exists(os.path.join(src_dir, "boid_simulation_grid.cpp")):
         return False
-    subprocess.run([os.path.join(HERE, "build_ref.sh"), src_dir], check=True,
-                   capture_output=True)
+    subprocess.run(["bash", BUILD_REF, src_dir], check=True, capture_output=True)
     return True
 
 

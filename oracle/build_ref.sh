@@ -5,10 +5,19 @@
 # Flags follow the reference's CMakeLists.txt (-std=c++11 -O3, OpenMP) plus
 # -ffp-contract=off so that an aarch64 host rounds like the x86 build.
 #
-# usage: oracle/build_ref.sh [REFERENCE_SRC_DIR]   (default /root/reference/src)
+# The reference checkout is $REF_ROOT (its engine sources $REF_SRC, default
+# $REF_ROOT/src).  This recipe is the one place that names the checkout's
+# default location; `build_ref.sh --root` prints the checkout it would use.
+#
+# usage: oracle/build_ref.sh [--root | REFERENCE_SRC_DIR]
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-src="${1:-${REF_SRC:-/root/reference/src}}"
+root="${REF_ROOT:-/root/reference}"
+if [ "${1:-}" = "--root" ]; then
+    echo "$root"
+    exit 0
+fi
+src="${1:-${REF_SRC:-$root/src}}"
 out="$here/_ref"
 if [ ! -f "$src/boid_simulation_grid.cpp" ]; then
     echo "build_ref.sh: reference sources not found at $src" >&2

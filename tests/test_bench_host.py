@@ -29,3 +29,46 @@ def test_clock_summary_without_samples():
     import bench
     c = bench.ClockSampler(0)
     assert c.summary() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+
+def _args(**kw):
+    import argparse
+    d = dict(n=2048, field=0.5, seed=777, engine="grid", allpairs_kernels=False, cpu_sample_steps=2)
+    d.update(kw)
+    return argparse.Namespace(**d)
+
+
+def test_both_arms_report_the_same_config(monkeypatch):
+    import bench
+    a = _args()
+    monkeypatch.delenv("WORLD_SIZE", raising=False)
+    c = bench.workload(a)
+    assert c == bench.workload(a) and c["parallelism"] == "single GPU" and c["kernels"] == "grid"
+    assert "flushed" in c["l2"]
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    assert bench.workload(a)["parallelism"] == "replicas"
+
+
+def test_cpu_baseline_parity_flag_counts_mismatches(oracle_mod):
+    """The in-bench parity check: the CPU baseline's updates from the timed
+    state against the GPU's, value by value (here the oracle stands in for
+    the GPU, once exact and once with two values planted wrong)."""
+    import numpy as np
+    import bench
+    O = oracle_mod
+    a = _args()
+    p = O.params(a.n, a.field, O.MARUN2019["sep"], O.MARUN2019["ali"], O.MARUN2019["coh"],
+                 O.MARUN2019["vmax"], O.MARUN2019["vmin"])
+    pos0, vel0 = O.init_state(p, "random_uniform", True, a.seed)
+    pos, vel = pos0.copy(), vel0.copy()
+    O.GridPort(p, pos).step(pos, vel, a.cpu_sample_steps)
+    out = bench.cpu_baseline_sample(a, pos0, vel0, (pos, vel))
+    assert out["parity"]["result"] == "bit-exact" and out["parity"]["mismatched_values"] == 0
+    assert out["parity"]["values"] == 6 * a.n and out["single_thread"]["cores"] == 1
+    assert out["value"] > 0 and out["single_thread"]["value"] > 0
+    bad = pos.copy()
+    bad[5] = np.nextafter(bad[5], np.float32(2))
+    badv = vel.copy()
+    badv[7] = -badv[7]
+    out = bench.cpu_baseline_sample(a, pos0, vel0, (bad, badv))
+    assert out["parity"]["result"] == "MISMATCH" and out["parity"]["mismatched_values"] == 2

@@ -23,7 +23,16 @@ import pytest
 from conftest import DATA, GOLDEN, make_params
 import ptcl_io
 
-REF_TOOLS = "/root/reference/tools"
+
+def _ref_dir(sub):
+    """A directory of the reference checkout (oracle.ref_root()), or None."""
+    import oracle
+    root = oracle.ref_root()
+    return os.path.join(root, sub) if root and os.path.isdir(os.path.join(root, sub)) else None
+
+
+REF_TOOLS = _ref_dir("tools")
+REF_SETTINGS = _ref_dir("settings")
 
 
 def run(exe, *args, cwd=None):
@@ -142,10 +151,10 @@ def _py_read_ini(path):
     return tree
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/settings"), reason="reference settings not here")
+@pytest.mark.skipif(REF_SETTINGS is None, reason="reference settings not here")
 def test_every_reference_settings_file_reads_the_same(cli):
     import glob
-    files = sorted(glob.glob("/root/reference/settings/**/*.ini", recursive=True))
+    files = sorted(glob.glob(os.path.join(REF_SETTINGS, "**", "*.ini"), recursive=True))
     assert files
     keys = {"separation_sight_distance": ("Separation", "SIGHT_DISTANCE"),
             "alignment_sight_angle": ("Alignment", "SIGHT_ANGLE"),
@@ -198,7 +207,7 @@ def test_oracle_frames_match_reference_digests(oracle_mod, name):
 def _import_swarm_util():
     """tools/swarm_util.py with its plotting imports stubbed (matplotlib,
     pandas and mpl_toolkits are not installed and not used by the readers)."""
-    path = os.path.join(REF_TOOLS, "swarm_util.py")
+    path = os.path.join(REF_TOOLS, "swarm_util.py") if REF_TOOLS else ""
     if not os.path.exists(path):
         pytest.skip("reference tools not present")
     class Anything(types.ModuleType):
