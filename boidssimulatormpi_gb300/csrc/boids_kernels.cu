@@ -982,35 +982,40 @@ __device__ uint64_t *block_radix_sort(uint64_t *a, uint64_t *b, uint32_t *hist, 
 
 constexpr int kDT = 128;                       // threads of k_grid_dense
 constexpr int kBufB = 24;                      // filter hits buffered per lane
-// Accepted neighbours the chunk lanes hand to their owners, 16-bit entries
-// (index | flags << 13).  The owners (chunk 0) keep theirs in registers, so
-// the kChunkPool entries are split over the nbr x (L - 1) other lanes:
-// kChunkPool / (nbr (L - 1)) >= 48 each, 96 when two lanes share a boid.
-// Entries are interleaved across lanes (entry-major).
-constexpr int kChunkPool = 6144;
-static_assert(kDenseCap <= (1 << 13), "a list entry holds the candidate index in 13 bits");
 constexpr int kDenseKT = kDenseCap / kDT;      // candidates per thread when the list is full
 
 constexpr int kMaxCuts = 32;                   // id windows of a huge cell planned at once
 
+// Accepted neighbours are marked in three bit masks per boid (cohesion,
+// separation, alignment) over the id-ordered candidate list; the ordered sums
+// then walk the masks.  kMaskWords words hold the masks of one round of
+// boids, so a round takes at most kMaskWords / (3 * words) boids.
+constexpr int kMaskWords = kDenseCap + 17 * kDT;
+// The per-boid results of the ordered sums of one round, in the storage of
+// the filter-hit buffers (dead by then): at most kSumsMax boids per round.
+constexpr int kSumsMax = (int)((kBufB * kDT * sizeof(uint16_t)) / sizeof(Acc));
+static_assert(kSumsMax >= 64, "a round holds a useful number of boids");
+
 // Shared memory of k_grid_dense.  Regions whose lifetimes do not overlap
-// share storage: the sort keys become the id-ordered candidate array, and the
-// gather slots and radix histogram become the chunk lists.
+// share storage: the sort keys become the id-ordered candidate array, the
+// gather slots and radix histogram become the rule masks, and the filter-hit
+// buffers become the per-boid sums.
 struct DenseSmem {
     union {
         uint64_t keys[2][kDenseCap];  // (id << 16) | (segment << 11) | gather index
-        float4 spos[kDenseCap];       // candidates in id order; w = slot | wrapped << 31
+        float4 spos[kDenseCap];       // candidates in id order, periodic images; w = slot
     } u;
     union {
         struct {
             uint32_t gslot[kDenseCap];      // state slot, by gather index
             uint32_t hist[17 * kDT];        // radix counters, padded (block_radix_sort)
         } s;
-        uint16_t lists[kChunkPool];         // per non-owner chunk lane: index | flags << 13
+        uint32_t masks[kMaskWords];         // rule r of round boid i: words (r * nbr + i) * wstride ...
     } v;
-    uint16_t bufs[kBufB * kDT];
-    uint16_t nlist[kDT];
-    uint8_t ovf[kDT];
+    union {
+        uint16_t bufs[kBufB * kDT];         // filter hits of each lane (candidate index), entry-major
+        Acc sums[kSumsMax];                 // the ordered sums of each boid of the round
+    } w;
     uint32_t seg_j0[18], seg_k0[19];
     float seg_s[18][3];
     uint32_t work, flock;
@@ -1027,15 +1032,114 @@ struct DenseSmem {
 };
 static_assert(kDenseCap <= 2048, "gather index must fit 11 bits");
 
-// The exact image of candidate q of the id-ordered list as seen from pi.
-// Non-wrapped candidates are stored with their exact coordinates and, being
-// nearer than F/2, are their own image; the few across a periodic face are
-// re-read and imaged as the reference does.
-__device__ __forceinline__ float3 cand_image(float4 c, float3 pi, const float4 *__restrict__ pos, const StepConst &k)
+// The candidates of the id-ordered list hold their periodic images as seen
+// from the cell, exactly as the reference computes them: a candidate of a
+// segment across a periodic face is shifted by the field size on that axis
+// ((float)((double)x -+ F)), the others are unshifted.  That is the
+// reference's own minimum image for every pair it can accept: such a pair is
+// nearer than the largest sight radius R, which is at most F/3 (at least 3
+// device cells per axis), so across a face the reference's test
+// |xj - xi| > F/2 holds (|xj - xi| > F - R) and inside the field it fails
+// (|xj - xi| < R).  Where the reference images a candidate otherwise, it is
+// farther than R from the boid in both placements and no rule accepts it.
+
+// The ordered sums of a round's boids run as jobs, each a (job, boid) pair
+// taken by one lane, job-major so that the lanes of a warp run the same code:
+// jobs 0-5 are the cohesion sum's x, y, z and the alignment sum's x, y, z
+// (jobs 0 and 3 also count), job 6 the separation sum (all three components,
+// from the normalised offsets), job 7 the neighbour-set id hashes
+// (diagnostics only).  Each walks its rule's mask word by word from candidate
+// 0 up: ascending id, the reference's order of accumulation, so every float
+// sum is the reference's sequence of additions.  A job's running value starts
+// from the earlier id windows' partial sums (carry) or zero, and ends in out.
+__device__ __forceinline__ void dense_sum_job(const DenseSmem &sm, const uint32_t *m, uint32_t words, uint32_t job,
+                                              const Acc *carry, Acc &out)
 {
-    const uint32_t w = __float_as_uint(c.w);
-    if (w >> 31) return image3(xyz(__ldg(pos + (w & 0x7fffffffu))), pi, k);
-    return xyz(c);
+    const bool coh = job < 3;
+    const uint32_t c = job % 3;
+    // the summands: the candidates' imaged positions, or their velocities
+    const float *base = coh ? reinterpret_cast<const float *>(sm.u.spos) + c
+                            : (c == 0 ? sm.svx : (c == 1 ? sm.svy : sm.svz));
+    const uint32_t sh = coh ? 2u : 0u;  // element q at base[q << sh]
+    float *dst = reinterpret_cast<float *>(&out) + (coh ? 0 : 6) + c;
+    float acc = carry ? reinterpret_cast<const float *>(carry)[(coh ? 0 : 6) + c] : 0.f;
+    int cnt = 0;
+    for (uint32_t w = 0; w < words; ++w) {
+        uint32_t bits = m[w];
+        cnt += __popc(bits);
+        const uint32_t q0 = w * 32;
+        // four entries per iteration: their loads in flight together, their
+        // additions in order
+        while (bits) {
+            const uint32_t b0 = (uint32_t)__ffs(bits) - 1;
+            bits &= bits - 1;
+            const bool h1 = bits != 0;
+            const uint32_t b1 = h1 ? (uint32_t)__ffs(bits) - 1 : b0;
+            bits &= bits - 1;
+            const bool h2 = bits != 0;
+            const uint32_t b2 = h2 ? (uint32_t)__ffs(bits) - 1 : b0;
+            bits &= bits - 1;
+            const bool h3 = bits != 0;
+            const uint32_t b3 = h3 ? (uint32_t)__ffs(bits) - 1 : b0;
+            bits &= bits - 1;
+            const float v0 = base[(q0 + b0) << sh], v1 = base[(q0 + b1) << sh];
+            const float v2 = base[(q0 + b2) << sh], v3 = base[(q0 + b3) << sh];
+            acc = __fadd_rn(acc, v0);
+            if (h1) acc = __fadd_rn(acc, v1);
+            if (h2) acc = __fadd_rn(acc, v2);
+            if (h3) acc = __fadd_rn(acc, v3);
+        }
+    }
+    *dst = acc;
+    if (c == 0) {
+        int *n = coh ? &out.ncoh : &out.nali;
+        *n = cnt + (carry ? (coh ? carry->ncoh : carry->nali) : 0);
+    }
+}
+
+// Job 6: the separation sum (Vector3D::normalized of pi - t, as acc_add).
+__device__ __forceinline__ void dense_sep_job(const DenseSmem &sm, const uint32_t *m, uint32_t words, float3 pi,
+                                              const Acc *carry, Acc &out)
+{
+    float3 sep = carry ? carry->sep : make_float3(0.f, 0.f, 0.f);
+    int cnt = carry ? carry->nsep : 0;
+    for (uint32_t w = 0; w < words; ++w) {
+        uint32_t bits = m[w];
+        cnt += __popc(bits);
+        while (bits) {
+            const uint32_t q = w * 32 + (uint32_t)(__ffs(bits) - 1);
+            bits &= bits - 1;
+            const float4 t = sm.u.spos[q];
+            const float dx = __fsub_rn(pi.x, t.x), dy = __fsub_rn(pi.y, t.y), dz = __fsub_rn(pi.z, t.z);
+            const float n = nrm3(dx, dy, dz);
+            sep.x = __fadd_rn(sep.x, __fdiv_rn(dx, n));
+            sep.y = __fadd_rn(sep.y, __fdiv_rn(dy, n));
+            sep.z = __fadd_rn(sep.z, __fdiv_rn(dz, n));
+        }
+    }
+    out.sep = sep;
+    out.nsep = cnt;
+}
+
+// Job 7 (diagnostics): the order-free id fingerprints of the three sets.
+__device__ __forceinline__ void dense_hash_job(const DenseSmem &sm, const uint32_t *m0, uint32_t rstride,
+                                               uint32_t words, const Acc *carry, Acc &out,
+                                               const float4 *__restrict__ pos)
+{
+    for (uint32_t r = 0; r < 3; ++r) {
+        const uint32_t *m = m0 + r * rstride;
+        uint64_t h = carry ? carry->h[r] : 0;
+        for (uint32_t w = 0; w < words; ++w) {
+            uint32_t bits = m[w];
+            while (bits) {
+                const uint32_t q = w * 32 + (uint32_t)(__ffs(bits) - 1);
+                bits &= bits - 1;
+                const uint32_t j = __float_as_uint(sm.u.spos[q].w);
+                h += id_hash(__float_as_uint(__ldg(&pos[j].w)));
+            }
+        }
+        out.h[r] = h;
+    }
 }
 
 // Id window of a huge cell (more than kDenseCap candidates): the largest hi
@@ -1170,15 +1274,16 @@ __device__ void dense_window_plan(DenseSmem &sm, const GridIn &g, int ns, uint32
 // One CTA takes one work item at a time (dynamic queue): a crowded cell and
 // up to 128 of its boids (a cell with more boids is several items, taken by
 // several CTAs).  The cell's 27-cell candidates are radix-sorted by id once
-// per item.  The item's b boids x the candidate list is then split over all
-// threads: each boid gets L = 128/b lanes, lane l walks chunk l of the
-// id-ordered list with the half-precision filter; chunk 0's lane (the owner)
-// accumulates its accepted neighbours at once, the others hand theirs over
-// in id order and the owner folds them in after its own, so the accumulation
-// order stays ascending id.  A chunk lane whose hand-over list overflows
-// leaves its chunk to the owner.  A cell with more than kDenseCap candidates
-// is done in ascending id windows that each fit the list; the owners carry
-// their partial sums from window to window through o.carry.
+// per item.  The item's boids go in rounds; the round's nbr boids x the
+// candidate list is split over all threads: each boid gets L = 128/nbr
+// lanes, lane l walks chunk l of the id-ordered list with the
+// half-precision filter and exact tests, and marks the accepted neighbours
+// in the boid's three rule masks (bit q = candidate q).  The ordered sums
+// then run as jobs, one float sum (or the separation sum) per lane of the
+// boid, each walking its mask from candidate 0 up: ascending id, as the
+// reference accumulates.  A cell with more than kDenseCap candidates is done
+// in ascending id windows that each fit the list; the sums are carried from
+// window to window through o.carry.
 template <bool DIAG, bool MULTI>
 __global__ void __launch_bounds__(kDT, 4)
 k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint32_t *__restrict__ dense_n,
@@ -1305,10 +1410,13 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                 if (q < (int)nw) {
                     const float4 p = __ldg(g.pos + slot_r[i]);
                     const float *sh = sm.seg_s[seg_r[i]];
-                    const bool wrapped = sh[0] != 0.f || sh[1] != 0.f || sh[2] != 0.f;
-                    sm.u.spos[q] = wrapped ? make_float4(p.x + sh[0], p.y + sh[1], p.z + sh[2],
-                                                         __uint_as_float(slot_r[i] | 0x80000000u))
-                                           : make_float4(p.x, p.y, p.z, __uint_as_float(slot_r[i]));
+                    // the candidate's periodic image as the reference computes
+                    // it, (float)((double)x -+ F) on each shifted axis
+                    float4 im = make_float4(p.x, p.y, p.z, __uint_as_float(slot_r[i]));
+                    if (sh[0] != 0.f) im.x = add_f32_f64_rn(p.x, k.Fsd, sh[0] < 0.f);
+                    if (sh[1] != 0.f) im.y = add_f32_f64_rn(p.y, k.Fsd, sh[1] < 0.f);
+                    if (sh[2] != 0.f) im.z = add_f32_f64_rn(p.z, k.Fsd, sh[2] < 0.f);
+                    sm.u.spos[q] = im;
                     const float4 v = __ldg(g.vel + slot_r[i]);
                     sm.svx[q] = v.x;
                     sm.svy[q] = v.y;
@@ -1327,27 +1435,26 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
             __syncthreads();
             const bool first = lo == 0, last = hi >= k.n;
 
-            static_assert(kDenseRound == kDT, "a work item is one round of boids");
-            for (uint32_t r0 = rbeg; r0 < min(b, rbeg + (uint32_t)kDenseRound); r0 += kDT) {
-                const uint32_t nbr = min(b - r0, (uint32_t)kDT);      // boids this round
+            // The item's boids go in rounds of nbr (as many as the rule masks
+            // and the per-boid sums hold); each boid of a round gets L lanes.
+            const uint32_t words = (nw + 31) / 32, wstride = words | 1u;  // odd: boids' words in other banks
+            const uint32_t pool_nbr = (uint32_t)kMaskWords / (3u * wstride);
+            const uint32_t rend = min(b, rbeg + (uint32_t)kDenseRound);
+            const uint32_t njobs = DIAG ? 8u : 7u;
+            for (uint32_t r0 = rbeg; r0 < rend;) {
+                const uint32_t nbr = min(min(rend - r0, (uint32_t)kDT), min((uint32_t)kSumsMax, pool_nbr));
                 const uint32_t L = (uint32_t)kDT / nbr;               // lanes per boid
                 const uint32_t csz = ((nw + L - 1) / L + 1) & ~1u;    // chunk length (even: whole pairs)
                 const bool act = (uint32_t)t < nbr * L;
                 const uint32_t bi = act ? (uint32_t)t % nbr : 0, l = act ? (uint32_t)t / nbr : 0;
                 const uint32_t k0 = act ? min(nw, l * csz) : 0, k1 = act ? min(nw, k0 + csz) : 0;
-                // list entries per non-owner lane; entry e of lane x = t - nbr sits at
-                // e * lw + x, so that lanes side by side use banks side by side
-                const uint32_t lw = nbr * (L - 1), lcap = L > 1 ? (uint32_t)kChunkPool / lw : 0;
+                uint32_t *masks = sm.v.masks;
+                for (uint32_t i = (uint32_t)t; i < 3 * nbr * wstride; i += kDT) masks[i] = 0;
                 const uint32_t s = own0 + r0 + bi;
                 const float4 p4 = g.pos[s], v4 = g.vel[s];
                 const float3 pi = xyz(p4), vi = xyz(v4);
                 const Sight sight = make_sight(vi);
-                const float dot_lim = k.cone_pre ? -(sight.nv * k.dot_eps) : -INFINITY;  // cone pre-test
-                Acc a;
-                if (act && l == 0 && !first) a = o.carry[s];  // the earlier windows' sums
-                else acc_zero(a);
-                int nb = 0, nl = 0;
-                bool ovf = false;
+                int nb = 0;
                 // The filter in half precision, two candidates per instruction:
                 // it keeps every pair within the filter radius and drops only
                 // pairs whose exact v . r is negative (the bounds are in hfilt,
@@ -1365,6 +1472,8 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                                                      : __ushort_as_half((unsigned short)0xfc00u));  // -inf
                 const uint32_t p0 = k0 >> 1, plen = k1 > k0 ? ((k1 + 1) >> 1) - p0 : 0;  // pairs
                 const uint32_t maxlen = __reduce_max_sync(0xffffffffu, plen);
+                uint32_t *mcoh = masks + bi * wstride, *msep = mcoh + nbr * wstride, *mali = msep + nbr * wstride;
+                __syncthreads();  // the masks are clear
                 for (uint32_t it = 0; it < maxlen; ++it) {
                     if (it < plen) {
                         const uint32_t pp = p0 + it;
@@ -1373,70 +1482,49 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                         const __half2 d2 = __hfma2(dz, dz, __hfma2(dy, dy, __hmul2(dx, dx)));
                         const __half2 dv = __hfma2(hvz, dz, __hfma2(hvy, dy, __hmul2(hvx, dx)));
                         const unsigned keep = __hlt2_mask(d2, hf2) & __hge2_mask(dv, hd2);
-                        if (keep & 0xffffu) sm.bufs[nb++ * kDT + t] = (uint16_t)(2 * pp);
-                        if (keep >> 16) sm.bufs[nb++ * kDT + t] = (uint16_t)(2 * pp + 1);
+                        if (keep & 0xffffu) sm.w.bufs[nb++ * kDT + t] = (uint16_t)(2 * pp);
+                        if (keep >> 16) sm.w.bufs[nb++ * kDT + t] = (uint16_t)(2 * pp + 1);
                     }
-                    // exact tests of the buffered hits, the whole warp together
+                    // exact tests of the buffered hits, the whole warp together;
+                    // accepted neighbours are marked in the boid's rule masks
                     if (__any_sync(0xffffffffu, nb >= kBufB - 1) || it + 1 == maxlen) {
                         for (int e = 0; e < nb; ++e) {
-                            const uint32_t q = sm.bufs[e * kDT + t];
+                            const uint32_t q = sm.w.bufs[e * kDT + t];
                             const float4 cq = sm.u.spos[q];
-                            const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
-                            if (j == s) continue;
-                            const float3 tt = cand_image(cq, pi, g.pos, k);
-                            const int f = pair_flags(pi, sight, tt, k);
+                            if (__float_as_uint(cq.w) == s) continue;
+                            const int f = pair_flags(pi, sight, xyz(cq), k);
                             if (!f) continue;
-                            if (l == 0) {
-                                const float3 vj = (f & 4) ? make_float3(sm.svx[q], sm.svy[q], sm.svz[q]) : make_float3(0.f, 0.f, 0.f);
-                                acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
-                            } else if ((uint32_t)nl < lcap) {
-                                sm.v.lists[nl++ * lw + (t - nbr)] = (uint16_t)(q | ((uint32_t)f << 13));
-                            } else {
-                                ovf = true;
-                            }
+                            const uint32_t bit = 1u << (q & 31), wq = q >> 5;
+                            if (f & 1) atomicOr(mcoh + wq, bit);
+                            if (f & 2) atomicOr(msep + wq, bit);
+                            if (f & 4) atomicOr(mali + wq, bit);
                         }
                         nb = 0;
                     }
                 }
-                sm.nlist[t] = (uint16_t)nl;
-                sm.ovf[t] = ovf;
+                __syncthreads();  // the masks are complete; the hit buffers are dead
+                for (uint32_t pj = (uint32_t)t; pj < njobs * nbr; pj += kDT) {
+                    const uint32_t job = pj / nbr, jb = pj - job * nbr;
+                    const uint32_t js = own0 + r0 + jb;
+                    const Acc *cin = first ? nullptr : o.carry + js;
+                    Acc &out = sm.w.sums[jb];
+                    if (job < 6) {
+                        dense_sum_job(sm, masks + ((job < 3 ? 0u : 2u) * nbr + jb) * wstride, words, job, cin, out);
+                    } else if (job == 6) {
+                        dense_sep_job(sm, masks + (nbr + jb) * wstride, words, xyz(g.pos[js]), cin, out);
+                    } else if (DIAG) {
+                        dense_hash_job(sm, masks + jb * wstride, nbr * wstride, words, cin, out, g.pos);
+                    }
+                }
                 __syncthreads();
                 if (act && l == 0) {
-                    // fold the other chunks' neighbours in, in chunk (= id) order
-                    for (uint32_t ll = 1; ll < L; ++ll) {
-                        const uint32_t tt_ = ll * nbr + bi;
-                        if (sm.ovf[tt_]) {
-                            const uint32_t c0 = min(nw, ll * csz), c1 = min(nw, c0 + csz);
-                            for (uint32_t q = c0; q < c1; ++q) {
-                                const float4 cq = sm.u.spos[q];
-                                const float dx = cq.x - pi.x, dy = cq.y - pi.y, dz = cq.z - pi.z;
-                                const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                                const float dv = __fmaf_rn(vi.z, dz, __fmaf_rn(vi.y, dy, __fmul_rn(vi.x, dx)));
-                                const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
-                                if (!(d2 < k.filt_r2) || !(dv >= dot_lim) || j == s) continue;
-                                const float3 tt = cand_image(cq, pi, g.pos, k);
-                                const int f = pair_flags(pi, sight, tt, k);
-                                if (!f) continue;
-                                const float3 vj = (f & 4) ? make_float3(sm.svx[q], sm.svy[q], sm.svz[q]) : make_float3(0.f, 0.f, 0.f);
-                                acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
-                            }
-                        } else {
-                            const uint32_t m = sm.nlist[tt_];
-                            for (uint32_t e = 0; e < m; ++e) {
-                                const uint32_t v = sm.v.lists[e * lw + (tt_ - nbr)];
-                                const float4 cq = sm.u.spos[v & 0x1fffu];
-                                const int f = (int)(v >> 13);
-                                const uint32_t j = __float_as_uint(cq.w) & 0x7fffffffu;
-                                const float3 tt = cand_image(cq, pi, g.pos, k);
-                                const float3 vj = (f & 4) ? make_float3(sm.svx[v & 0x1fffu], sm.svy[v & 0x1fffu], sm.svz[v & 0x1fffu]) : make_float3(0.f, 0.f, 0.f);
-                                acc_add<DIAG>(a, pi, tt, vj, f, DIAG ? __float_as_uint(__ldg(&g.pos[j].w)) : 0u);
-                            }
-                        }
-                    }
+                    Acc a = sm.w.sums[bi];
+                    if (!DIAG) a.h[0] = a.h[1] = a.h[2] = 0;
                     if (last) finish_boid<DIAG>(a, p4, vi, s, o, k);
                     else o.carry[s] = a;
                 }
-                __syncthreads();  // lists and buffers are reused by the next round
+                __syncthreads();  // masks and sums are reused by the next round
+                r0 += nbr;
             }
             if (last) break;
             lo = hi;

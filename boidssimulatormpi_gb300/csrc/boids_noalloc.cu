@@ -18,7 +18,12 @@
 //    (about 370 000 boids at the reference's density);
 //  * all calls share the one array: two calls whose GPU work overlaps in time
 //    (different streams, or different host threads on one device) race and
-//    corrupt each other's results; order them on one stream.
+//    corrupt each other's results; order them on one stream;
+//  * the first call on a device loads the library's device code there (lazy
+//    module loading), so make it before any stream capture.
+// Each call looks the array's address up in the current context, keeps the
+// step constants of the last few parameter sets in fixed host storage, and
+// leaves the caller's current device as it found it.
 #include "boids.h"
 #include "boids_engine.h"
 
@@ -33,33 +38,101 @@ int grid_constants_noalloc(const boids_params *params, StepConst *out);
 }  // namespace boidsgpu
 
 // The scratch.  In host code this name only stands for the symbol; its device
-// address comes from cudaGetSymbolAddress, once per device.
+// address comes from cudaGetSymbolAddress with the device current.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[BOIDS_NOALLOC_SCRATCH_BYTES];
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-unsigned char *g_scratch_addr[kMaxDevices];  // device address of the array, per device
-
-// Device address of the scratch on `dev`, which must be the current device.
-// The first call on a device looks it up; later calls reuse it.
-int scratch_address(int dev, unsigned char **out)
+// Device address of the scratch in the current device's context, looked up
+// on every call: a host-side lookup of microseconds, and never stale (a
+// cached address would outlive a cudaDeviceReset, after which the module is
+// loaded again into a new context).
+int scratch_address(unsigned char **out)
 {
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) {
-            char msg[160];
-            std::snprintf(msg, sizeof msg, "boids_step_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-            return boidsgpu::set_last_error(BOIDS_ECUDA, msg);
-        }
-        g_scratch_addr[dev] = static_cast<unsigned char *>(p);
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+        char msg[160];
+        std::snprintf(msg, sizeof msg, "boids_step_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        return boidsgpu::set_last_error(BOIDS_ECUDA, msg);
     }
-    *out = g_scratch_addr[dev];
+    *out = static_cast<unsigned char *>(p);
     return BOIDS_OK;
 }
+
+// The step constants of the last few parameter sets.  Deriving them runs a
+// bisection with the host's acosf and a monotonicity check around it (about
+// 0.2 ms); a loop that steps the same flock call after call finds them here.
+// Fixed storage, no allocation; the fields are compared one by one, so
+// padding bytes never matter.
+constexpr int kConstCache = 4;
+struct ConstEntry {
+    bool used;
+    boids_params p;
+    boidsgpu::StepConst k;
+};
+std::mutex g_const_mutex;
+ConstEntry g_const_cache[kConstCache];
+int g_const_next;
+
+bool same_params(const boids_params &a, const boids_params &b)
+{
+    return a.number_of_agents == b.number_of_agents && a.field_size == b.field_size &&
+           a.separation_sight_distance == b.separation_sight_distance &&
+           a.separation_sight_angle == b.separation_sight_angle &&
+           a.separation_force_coefficient == b.separation_force_coefficient &&
+           a.alignment_sight_distance == b.alignment_sight_distance &&
+           a.alignment_sight_angle == b.alignment_sight_angle &&
+           a.alignment_force_coefficient == b.alignment_force_coefficient &&
+           a.cohesion_sight_distance == b.cohesion_sight_distance &&
+           a.cohesion_sight_angle == b.cohesion_sight_angle &&
+           a.cohesion_force_coefficient == b.cohesion_force_coefficient && a.velocity_max == b.velocity_max &&
+           a.velocity_min == b.velocity_min && a.engine == b.engine && a.flags == b.flags;
+}
+
+int step_constants(const boids_params *params, boidsgpu::StepConst *out)
+{
+    {
+        std::lock_guard<std::mutex> lock(g_const_mutex);
+        for (const ConstEntry &e : g_const_cache) {
+            if (e.used && same_params(e.p, *params)) {
+                *out = e.k;
+                return BOIDS_OK;
+            }
+        }
+    }
+    boidsgpu::StepConst k;
+    const int rc = boidsgpu::grid_constants_noalloc(params, &k);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(g_const_mutex);
+    ConstEntry &e = g_const_cache[g_const_next];
+    g_const_next = (g_const_next + 1) % kConstCache;
+    e.used = true;
+    e.p = *params;
+    e.k = k;
+    *out = k;
+    return BOIDS_OK;
+}
+
+// Makes `dev` current for the life of the object and gives the caller's
+// current device back at the end.
+struct DeviceScope {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceScope(int dev)
+    {
+        if ((err = cudaGetDevice(&prev)) != cudaSuccess) {
+            prev = -1;
+            return;
+        }
+        if (prev != dev) err = cudaSetDevice(dev);
+    }
+    ~DeviceScope()
+    {
+        int now = -1;
+        if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
+    }
+};
 
 size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -104,10 +177,10 @@ extern "C" int boids_step_noalloc(const boids_params *params, const float *pos3n
     const uint32_t n = params->number_of_agents;
     if (n && (!pos3n_in || !vel3n_in || !pos3n_out || !vel3n_out))
         return boidsgpu::set_last_error(BOIDS_EINVAL, "boids_step_noalloc: null state pointer");
-    if (params->device < 0 || params->device >= kMaxDevices)
+    if (params->device < 0)
         return boidsgpu::set_last_error(BOIDS_EINVAL, "boids_step_noalloc: bad device ordinal");
     boidsgpu::StepConst k;
-    int rc = boidsgpu::grid_constants_noalloc(params, &k);
+    int rc = step_constants(params, &k);
     if (rc) return rc;
     boidsgpu::DevBuffers b{};
     const size_t need = layout(k, nullptr, &b);
@@ -119,10 +192,11 @@ extern "C" int boids_step_noalloc(const boids_params *params, const float *pos3n
                       need, (unsigned)BOIDS_NOALLOC_SCRATCH_BYTES);
         return boidsgpu::set_last_error(BOIDS_EINVAL, msg);
     }
-    cudaError_t e = cudaSetDevice(params->device);
+    DeviceScope scope(params->device);
+    cudaError_t e = scope.err;
     if (e != cudaSuccess) return boidsgpu::set_last_error(BOIDS_ECUDA, cudaGetErrorString(e));
     unsigned char *base = nullptr;
-    if ((rc = scratch_address(params->device, &base))) return rc;
+    if ((rc = scratch_address(&base))) return rc;
     layout(k, base, &b);
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, params->device);

@@ -320,10 +320,14 @@ int boids_mlp_train(boids_mlp *mlp, const float *x, const float *target, int32_t
  * All scratch lives in one static device array of BOIDS_NOALLOC_SCRATCH_BYTES
  * that every GPU loading the library holds until the process exits; a step
  * needing more (roughly 370 000 boids at the reference's density) returns
- * BOIDS_EINVAL.  The first call on a device looks up the array's device
- * address, so make that first call before any stream capture.  Every call
- * shares the array: calls whose GPU work overlaps (other streams, other
- * threads on the same device) race; order them on one stream.  The work is
+ * BOIDS_EINVAL.  Each call looks the array's device address up in the
+ * current context (a host-side lookup, so a device reset between calls does
+ * no harm); the first call on a device also loads the library's device code
+ * there, so make that first call before any stream capture.  Every call
+ * shares the array and clears what must start at zero: calls whose GPU work
+ * overlaps (other streams, other threads on the same device) race; order
+ * them on one stream.  params->device is made current for the call and the
+ * caller's current device is restored before it returns.  The work is
  * queued on cuda_stream (a cudaStream_t; NULL is the legacy default stream)
  * and the call returns without waiting for it. */
 int boids_step_noalloc(const boids_params *params, const float *pos3n_in, const float *vel3n_in,

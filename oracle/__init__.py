@@ -191,12 +191,15 @@ def ref_available(kind: str = "grid") -> bool:
 
 
 class RefEngine:
-    """BoidSimulation from the reference's own sources (kind 'grid' or 'allpairs')."""
+    """BoidSimulation from the reference's own sources (kind 'grid' or
+    'allpairs'), through the ref_* shim of ref_driver.cpp.  lib_path names
+    another build of that shim (the same driver linked against another
+    BoidSimulation, e.g. the GB300 engine's C++ adapter)."""
 
     _libs: dict = {}
 
-    def __init__(self, kind, p: OrcParams, init="random_uniform", seed=12345):
-        L = self._load(kind)
+    def __init__(self, kind, p: OrcParams, init="random_uniform", seed=12345, lib_path=None):
+        L = self._load(kind, lib_path)
         self.L, self.n = L, p.n
         self.h = L.ref_create(p.n, p.field, p.sep_r, p.sep_a, p.sep_c, p.ali_r, p.ali_a,
                               p.ali_c, p.coh_r, p.coh_a, p.coh_c, p.vmax, p.vmin,
@@ -204,9 +207,10 @@ class RefEngine:
         self.kind = kind
 
     @classmethod
-    def _load(cls, kind):
-        if kind not in cls._libs:
-            path = os.path.join(REF_DIR, "libref_%s.so" % kind)
+    def _load(cls, kind, lib_path=None):
+        key = lib_path or kind
+        if key not in cls._libs:
+            path = lib_path or os.path.join(REF_DIR, "libref_%s.so" % kind)
             if not os.path.exists(path):
                 raise FileNotFoundError(path)
             L = C.CDLL(path)
@@ -221,8 +225,8 @@ class RefEngine:
             L.ref_get_force.argtypes = [C.c_void_p, _f32p]
             L.ref_get_grid_index.argtypes = [C.c_void_p, _i32p]
             L.ref_grid_num.argtypes = [C.c_void_p]
-            cls._libs[kind] = L
-        return cls._libs[kind]
+            cls._libs[key] = L
+        return cls._libs[key]
 
     def init(self, fresh_drand48=False):
         """BoidSimulation::init.  fresh_drand48 resets glibc's drand48 state to
