@@ -980,6 +980,96 @@ __device__ uint64_t *block_radix_sort(uint64_t *a, uint64_t *b, uint32_t *hist, 
     return a;
 }
 
+// Sort of n (<= kDenseCap) 64-bit keys (id << 16 | payload) by id, ids
+// distinct: one bucket pass over the ids' actual range, then each key's place
+// inside its bucket by counting the smaller ids there.  Keys whose ids bunch
+// into a few buckets (more than kBucketMax in one) go to the radix sort
+// instead, so the result never depends on the id distribution and the cost
+// never grows quadratically.  NT threads; `cnt` holds kBuckets + 1 words.
+// Returns the buffer that holds the sorted keys.
+constexpr int kBuckets = 512;
+constexpr int kBucketMax = 24;
+
+template <int NT>
+__device__ uint64_t *block_bucket_sort(uint64_t *a, uint64_t *b, uint32_t *cnt, int n, int id_bits)
+{
+    static_assert(kBuckets % NT == 0, "buckets per thread");
+    constexpr int kPer = kBuckets / NT;
+    __shared__ uint32_t red[2][NT / 32];
+    __shared__ uint32_t info[2];  // id shift, largest bucket
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    // the ids' range
+    uint32_t mn = 0xffffffffu, mx = 0;
+    for (int i = t; i < n; i += NT) {
+        const uint32_t id = (uint32_t)(a[i] >> 16);
+        mn = min(mn, id);
+        mx = max(mx, id);
+    }
+    mn = __reduce_min_sync(0xffffffffu, mn);
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if (lane == 0) { red[0][wid] = mn; red[1][wid] = mx; }
+    for (int i = t; i <= kBuckets; i += NT) cnt[i] = 0;
+    __syncthreads();
+    mn = red[0][0];
+    mx = red[1][0];
+#pragma unroll
+    for (int w = 1; w < NT / 32; ++w) { mn = min(mn, red[0][w]); mx = max(mx, red[1][w]); }
+    // bucket = (id - mn) >> shift, shift the least with range >> shift < kBuckets
+    const uint32_t range = n > 0 ? mx - mn : 0;
+    const int shift = range < (uint32_t)kBuckets ? 0 : 32 - __clz(range) - 9;  // kBuckets = 2^9
+    // each key's rank among its bucket's arrivals, and the bucket counts
+    uint32_t rk[kDenseCap / NT], bk[kDenseCap / NT];
+#pragma unroll
+    for (int r = 0; r < kDenseCap / NT; ++r) {
+        const int i = t + r * NT;
+        if (i < n) {
+            bk[r] = ((uint32_t)(a[i] >> 16) - mn) >> shift;
+            rk[r] = atomicAdd(&cnt[bk[r]], 1u);
+        }
+    }
+    __syncthreads();
+    // exclusive scan of the counts; the largest bucket
+    uint32_t loc[kPer], sum = 0, big = 0;
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) { loc[q] = cnt[t * kPer + q]; sum += loc[q]; big = max(big, loc[q]); }
+    big = __reduce_max_sync(0xffffffffu, big);
+    if (lane == 0) red[1][wid] = big;
+    uint32_t total;
+    uint32_t pre = block_excl_scan<NT>(sum, red[0], total);
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) { cnt[t * kPer + q] = pre; pre += loc[q]; }
+    if (t == 0) {
+        uint32_t m = 0;
+#pragma unroll
+        for (int w = 0; w < NT / 32; ++w) m = max(m, red[1][w]);
+        info[1] = m;
+    }
+    if (t == NT - 1) cnt[kBuckets] = pre;
+    __syncthreads();
+    if (info[1] > (uint32_t)kBucketMax) return block_radix_sort<NT>(a, b, cnt, n, 16, id_bits);
+    // file the keys by bucket, then place each inside its bucket
+#pragma unroll
+    for (int r = 0; r < kDenseCap / NT; ++r) {
+        const int i = t + r * NT;
+        if (i < n) b[cnt[bk[r]] + rk[r]] = a[i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kDenseCap / NT; ++r) {
+        const int i = t + r * NT;
+        if (i < n) {
+            const uint32_t b0 = cnt[bk[r]], b1 = cnt[bk[r] + 1];
+            const uint64_t key = b[b0 + rk[r]];
+            const uint32_t id = (uint32_t)(key >> 16);
+            uint32_t below = 0;
+            for (uint32_t j = b0; j < b1; ++j) below += (uint32_t)(b[j] >> 16) < id;
+            a[b0 + below] = key;
+        }
+    }
+    __syncthreads();
+    return a;
+}
+
 constexpr int kDT = 128;                       // threads of k_grid_dense
 constexpr int kBufB = 24;                      // filter hits buffered per lane
 constexpr int kDenseKT = kDenseCap / kDT;      // candidates per thread when the list is full
@@ -1388,7 +1478,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                 __syncthreads();
             }
             const uint64_t *sorted =
-                block_radix_sort<kDT>(sm.u.keys[0], sm.u.keys[1], sm.v.s.hist, (int)nw, 16, k.id_bits);
+                block_bucket_sort<kDT>(sm.u.keys[0], sm.u.keys[1], sm.v.s.hist, (int)nw, k.id_bits);
             // lay the candidates out in id order over the dead sort buffers
             // (thread t takes positions t, t + kDT, ...: no bank conflicts)
             const float3 cen = make_float3(((float)cx + 0.5f) * k.side, ((float)cy + 0.5f) * k.side,

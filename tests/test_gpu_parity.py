@@ -603,3 +603,32 @@ def test_c_caller_frames_equal_the_oracle(capi_caller, oracle_mod, tmp_path, eng
     assert_bits_equal(tail[:3 * n], pos, "final positions")
     assert_bits_equal(tail[3 * n:6 * n], vel, "final velocities")
     assert_bits_equal(tail[6 * n:], f, "forces of the last update")
+
+
+def test_crowded_cell_with_bunched_ids(boids_lib, oracle_mod):
+    """A crowded cell whose boids' ids bunch at both ends of the id range
+    (0..149 and N-150..N-1): the CTA-per-cell kernel's id sort sees a few
+    buckets holding most of its candidates and takes its radix path; the
+    cells elsewhere take the bucket path.  Three updates against the oracle."""
+    O = oracle_mod
+    rng = np.random.default_rng(7)
+    n, field = 65536, 1.6
+    prm = O.MARUN2019
+    p = make_params(O, n, field, prm)
+    pos = rng.random((n, 3)) * field
+    crowd = np.r_[np.arange(150), np.arange(n - 150, n)]
+    d = rng.normal(size=(crowd.size, 3))
+    d *= (0.02 * rng.uniform(0, 1, (crowd.size, 1)) ** (1 / 3)) / np.linalg.norm(d, axis=1, keepdims=True)
+    pos[crowd] = 0.8 + d
+    pos = pos.astype(np.float32).reshape(-1)
+    v = rng.normal(size=(n, 3))
+    vel = (v * rng.uniform(0.001, 0.005, (n, 1)) / np.linalg.norm(v, axis=1, keepdims=True))
+    vel = vel.astype(np.float32).reshape(-1)
+    sim = make_sim(boids_lib, "grid", n, field, prm)
+    sim.set_state(pos, vel)
+    sim.update(3)
+    op, ov, of = _oracle_run(O, p, "grid", pos, vel, 3)
+    gp, gv = sim.state()
+    assert_bits_equal(gp, op, "positions")
+    assert_bits_equal(gv, ov, "velocities")
+    assert_bits_equal(sim.forces(), of, "forces")
