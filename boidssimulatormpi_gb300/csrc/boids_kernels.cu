@@ -1071,7 +1071,6 @@ __device__ uint64_t *block_bucket_sort(uint64_t *a, uint64_t *b, uint32_t *cnt, 
 }
 
 constexpr int kDT = 128;                       // threads of k_grid_dense
-constexpr int kBufB = 24;                      // filter hits buffered per lane
 constexpr int kDenseKT = kDenseCap / kDT;      // candidates per thread when the list is full
 
 constexpr int kMaxCuts = 32;                   // id windows of a huge cell planned at once
@@ -1081,10 +1080,12 @@ constexpr int kMaxCuts = 32;                   // id windows of a huge cell plan
 // then walk the masks.  kMaskWords words hold the masks of one round of
 // boids, so a round takes at most kMaskWords / (3 * words) boids.
 constexpr int kMaskWords = kDenseCap + 17 * kDT;
-// The per-boid results of the ordered sums of one round, in the storage of
-// the filter-hit buffers (dead by then): at most kSumsMax boids per round.
-constexpr int kSumsMax = (int)((kBufB * kDT * sizeof(uint16_t)) / sizeof(Acc));
-static_assert(kSumsMax >= 64, "a round holds a useful number of boids");
+// At most kSumsMax boids per round: the per-boid table of the exact tests and
+// the per-boid results of the ordered sums hold that many.
+constexpr int kSumsMax = 85;
+// Filter hits queued per warp for the exact tests: a filter iteration adds at
+// most two per lane, so the queue is flushed once it holds kQueue - 64.
+constexpr int kQueue = 256;
 
 // Shared memory of k_grid_dense.  Regions whose lifetimes do not overlap
 // share storage: the sort keys become the id-ordered candidate array, the
@@ -1103,8 +1104,11 @@ struct DenseSmem {
         uint32_t masks[kMaskWords];         // rule r of round boid i: words (r * nbr + i) * wstride ...
     } v;
     union {
-        uint16_t bufs[kBufB * kDT];         // filter hits of each lane (candidate index), entry-major
-        Acc sums[kSumsMax];                 // the ordered sums of each boid of the round
+        struct {
+            uint32_t queue[kDT / 32][kQueue];  // per warp: filter hits, round boid << 11 | candidate
+            float4 obs[2][kSumsMax];           // per round boid: (position, |v|), (velocity, 1/|v|)
+        } a;
+        Acc sums[kSumsMax];                    // the ordered sums of each boid of the round
     } w;
     uint32_t seg_j0[18], seg_k0[19];
     float seg_s[18][3];
@@ -1540,56 +1544,79 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                 const uint32_t k0 = act ? min(nw, l * csz) : 0, k1 = act ? min(nw, k0 + csz) : 0;
                 uint32_t *masks = sm.v.masks;
                 for (uint32_t i = (uint32_t)t; i < 3 * nbr * wstride; i += kDT) masks[i] = 0;
-                const uint32_t s = own0 + r0 + bi;
-                const float4 p4 = g.pos[s], v4 = g.vel[s];
-                const float3 pi = xyz(p4), vi = xyz(v4);
-                const Sight sight = make_sight(vi);
-                int nb = 0;
-                // The filter in half precision, two candidates per instruction:
-                // it keeps every pair within the filter radius and drops only
-                // pairs whose exact v . r is negative (the bounds are in hfilt,
-                // hdot0 and hdot1); the exact tests decide the rest.
-                const __half2 bx = __float2half2_rn((pi.x - cen.x) * k.hsc);
-                const __half2 by = __float2half2_rn((pi.y - cen.y) * k.hsc);
-                const __half2 bz = __float2half2_rn((pi.z - cen.z) * k.hsc);
-                const float vt = sight.nv * k.hvsc;
-                const bool pre = k.cone_pre && vt <= 1.0f;
-                const __half2 hvx = __float2half2_rn(pre ? vi.x * k.hvsc : 0.f);
-                const __half2 hvy = __float2half2_rn(pre ? vi.y * k.hvsc : 0.f);
-                const __half2 hvz = __float2half2_rn(pre ? vi.z * k.hvsc : 0.f);
-                const __half2 hf2 = __half2half2(__float2half_ru(k.hfilt));
-                const __half2 hd2 = __half2half2(pre ? __float2half_rd(-(k.hdot0 + k.hdot1 * vt))
-                                                     : __ushort_as_half((unsigned short)0xfc00u));  // -inf
-                const uint32_t p0 = k0 >> 1, plen = k1 > k0 ? ((k1 + 1) >> 1) - p0 : 0;  // pairs
-                const uint32_t maxlen = __reduce_max_sync(0xffffffffu, plen);
-                uint32_t *mcoh = masks + bi * wstride, *msep = mcoh + nbr * wstride, *mali = msep + nbr * wstride;
-                __syncthreads();  // the masks are clear
-                for (uint32_t it = 0; it < maxlen; ++it) {
-                    if (it < plen) {
+                // the round's boids, for the filter constants and the exact tests
+                for (uint32_t i = (uint32_t)t; i < nbr; i += kDT) {
+                    const float4 pp = g.pos[own0 + r0 + i], vv = g.vel[own0 + r0 + i];
+                    const Sight sg = make_sight(xyz(vv));
+                    sm.w.a.obs[0][i] = make_float4(pp.x, pp.y, pp.z, sg.nv);
+                    sm.w.a.obs[1][i] = make_float4(vv.x, vv.y, vv.z, sg.inv_nv);
+                }
+                __syncthreads();  // the masks are clear, the table is written
+                {
+                    const float4 o0 = sm.w.a.obs[0][bi], o1 = sm.w.a.obs[1][bi];
+                    const float3 pi = xyz(o0), vi = xyz(o1);
+                    // The filter in half precision, two candidates per instruction:
+                    // it keeps every pair within the filter radius and drops only
+                    // pairs whose exact v . r is negative (the bounds are in hfilt,
+                    // hdot0 and hdot1); the exact tests decide the rest.
+                    const __half2 bx = __float2half2_rn((pi.x - cen.x) * k.hsc);
+                    const __half2 by = __float2half2_rn((pi.y - cen.y) * k.hsc);
+                    const __half2 bz = __float2half2_rn((pi.z - cen.z) * k.hsc);
+                    const float vt = o0.w * k.hvsc;
+                    const bool pre = k.cone_pre && vt <= 1.0f;
+                    const __half2 hvx = __float2half2_rn(pre ? vi.x * k.hvsc : 0.f);
+                    const __half2 hvy = __float2half2_rn(pre ? vi.y * k.hvsc : 0.f);
+                    const __half2 hvz = __float2half2_rn(pre ? vi.z * k.hvsc : 0.f);
+                    const __half2 hf2 = __half2half2(__float2half_ru(k.hfilt));
+                    const __half2 hd2 = __half2half2(pre ? __float2half_rd(-(k.hdot0 + k.hdot1 * vt))
+                                                         : __ushort_as_half((unsigned short)0xfc00u));  // -inf
+                    const uint32_t p0 = k0 >> 1, plen = k1 > k0 ? ((k1 + 1) >> 1) - p0 : 0;  // pairs
+                    const uint32_t maxlen = __reduce_max_sync(0xffffffffu, plen);
+                    const int lane = t & 31;
+                    const unsigned below = (1u << lane) - 1u;
+                    uint32_t *queue = sm.w.a.queue[t >> 5];
+                    uint32_t qlen = 0;  // the same in every lane of the warp
+                    for (uint32_t it = 0; it < maxlen; ++it) {
+                        bool h0 = false, h1 = false;
                         const uint32_t pp = p0 + it;
-                        const __half2 dx = __hsub2(sm.hx[pp], bx), dy = __hsub2(sm.hy[pp], by),
-                                      dz = __hsub2(sm.hz[pp], bz);
-                        const __half2 d2 = __hfma2(dz, dz, __hfma2(dy, dy, __hmul2(dx, dx)));
-                        const __half2 dv = __hfma2(hvz, dz, __hfma2(hvy, dy, __hmul2(hvx, dx)));
-                        const unsigned keep = __hlt2_mask(d2, hf2) & __hge2_mask(dv, hd2);
-                        if (keep & 0xffffu) sm.w.bufs[nb++ * kDT + t] = (uint16_t)(2 * pp);
-                        if (keep >> 16) sm.w.bufs[nb++ * kDT + t] = (uint16_t)(2 * pp + 1);
-                    }
-                    // exact tests of the buffered hits, the whole warp together;
-                    // accepted neighbours are marked in the boid's rule masks
-                    if (__any_sync(0xffffffffu, nb >= kBufB - 1) || it + 1 == maxlen) {
-                        for (int e = 0; e < nb; ++e) {
-                            const uint32_t q = sm.w.bufs[e * kDT + t];
-                            const float4 cq = sm.u.spos[q];
-                            if (__float_as_uint(cq.w) == s) continue;
-                            const int f = pair_flags(pi, sight, xyz(cq), k);
-                            if (!f) continue;
-                            const uint32_t bit = 1u << (q & 31), wq = q >> 5;
-                            if (f & 1) atomicOr(mcoh + wq, bit);
-                            if (f & 2) atomicOr(msep + wq, bit);
-                            if (f & 4) atomicOr(mali + wq, bit);
+                        if (it < plen) {
+                            const __half2 dx = __hsub2(sm.hx[pp], bx), dy = __hsub2(sm.hy[pp], by),
+                                          dz = __hsub2(sm.hz[pp], bz);
+                            const __half2 d2 = __hfma2(dz, dz, __hfma2(dy, dy, __hmul2(dx, dx)));
+                            const __half2 dv = __hfma2(hvz, dz, __hfma2(hvy, dy, __hmul2(hvx, dx)));
+                            const unsigned keep = __hlt2_mask(d2, hf2) & __hge2_mask(dv, hd2);
+                            h0 = (keep & 0xffffu) != 0;
+                            h1 = (keep >> 16) != 0;
                         }
-                        nb = 0;
+                        const unsigned b0 = __ballot_sync(0xffffffffu, h0), b1 = __ballot_sync(0xffffffffu, h1);
+                        if (h0) queue[qlen + __popc(b0 & below)] = (bi << 11) | (2 * pp);
+                        if (h1) queue[qlen + __popc(b0) + __popc(b1 & below)] = (bi << 11) | (2 * pp + 1);
+                        qlen += __popc(b0) + __popc(b1);
+                        // exact tests of the queued hits, every lane of the warp
+                        // busy; accepted neighbours are marked in the boid's masks
+                        if (qlen > (uint32_t)(kQueue - 64) || it + 1 == maxlen) {
+                            __syncwarp();
+                            for (uint32_t e = (uint32_t)lane; e < qlen; e += 32) {
+                                const uint32_t en = queue[e];
+                                const uint32_t eb = en >> 11, q = en & 0x7ffu;
+                                const float4 cq = sm.u.spos[q];
+                                if (__float_as_uint(cq.w) == own0 + r0 + eb) continue;
+                                const float4 a0 = sm.w.a.obs[0][eb], a1 = sm.w.a.obs[1][eb];
+                                Sight sg;
+                                sg.v = xyz(a1);
+                                sg.nv = a0.w;
+                                sg.inv_nv = a1.w;
+                                const int f = pair_flags(xyz(a0), sg, xyz(cq), k);
+                                if (!f) continue;
+                                uint32_t *mb = masks + eb * wstride + (q >> 5);
+                                const uint32_t bit = 1u << (q & 31);
+                                if (f & 1) atomicOr(mb, bit);
+                                if (f & 2) atomicOr(mb + nbr * wstride, bit);
+                                if (f & 4) atomicOr(mb + 2 * nbr * wstride, bit);
+                            }
+                            __syncwarp();
+                            qlen = 0;
+                        }
                     }
                 }
                 __syncthreads();  // the masks are complete; the hit buffers are dead
@@ -1608,9 +1635,10 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                 }
                 __syncthreads();
                 if (act && l == 0) {
+                    const uint32_t s = own0 + r0 + bi;
                     Acc a = sm.w.sums[bi];
                     if (!DIAG) a.h[0] = a.h[1] = a.h[2] = 0;
-                    if (last) finish_boid<DIAG>(a, p4, vi, s, o, k);
+                    if (last) finish_boid<DIAG>(a, g.pos[s], xyz(g.vel[s]), s, o, k);
                     else o.carry[s] = a;
                 }
                 __syncthreads();  // masks and sums are reused by the next round
