@@ -523,7 +523,7 @@ int boids_create(const boids_params *params, boids_sim **out)
         }
         int nsm = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p.device);
-        b.dense_grid = (uint32_t)std::max(1, nsm) * 4;
+        b.dense_grid = (uint32_t)std::max(1, nsm) * boidsgpu::kDenseCtasPerSm;
         b.wcap = (uint32_t)std::min<size_t>(boidsgpu::kWinScratch, std::max<size_t>(n, 1));
         ALLOC(&b.wscratch, (size_t)b.wcap * b.dense_grid);
     }

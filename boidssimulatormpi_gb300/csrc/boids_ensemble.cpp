@@ -298,7 +298,7 @@ int boids_ensemble_create(const boids_flock_desc *flocks, uint32_t count, boids_
     ALLOC(&e->d_err, 1);
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, e->device);
-    b.dense_grid = (uint32_t)std::max(1, nsm) * 4;
+    b.dense_grid = (uint32_t)std::max(1, nsm) * boidsgpu::kDenseCtasPerSm;
     {
         uint32_t nmax = 1;
         for (const auto &k : e->ks) nmax = std::max(nmax, k.n);

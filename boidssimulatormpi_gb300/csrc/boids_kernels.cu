@@ -941,38 +941,43 @@ k_grid_sparse_more(GridIn g, GridOut o, StepConst kp, FlockTable ft)
 // ------------------------------------------------------------------ dense cells: CTA per cell
 
 // Stable LSD radix sort of n 64-bit keys held in shared memory, on bits
-// [lo, lo + nbits), 4 bits per pass; NT threads each own a contiguous run.
-// hist holds 17 * NT words: counter i lives at i + i / 16, so that both the
-// (digit, thread) column walks and the thread-contiguous scan are free of
-// bank conflicts.  Returns the buffer that holds the sorted keys.
+// [lo, lo + nbits), kRadixBits bits per pass; NT threads each own a
+// contiguous run.  hist holds kRadixWords(NT) words: counter i lives at
+// i + i / 16, which keeps the (digit, thread) column walks free of bank
+// conflicts.  Returns the buffer that holds the sorted keys.  It is the
+// CTA-per-cell kernel's fallback sort (block_bucket_sort), so it favours a
+// small counter table over few passes.
 __device__ __forceinline__ int hpad(int i) { return i + (i >> 4); }
+constexpr int kRadixBits = 2, kRadixDigits = 1 << kRadixBits;
+__host__ __device__ constexpr int kRadixWords(int nt) { return kRadixDigits * nt + kRadixDigits * nt / 16; }
 
 template <int NT>
 __device__ uint64_t *block_radix_sort(uint64_t *a, uint64_t *b, uint32_t *hist, int n, int lo, int nbits)
 {
     __shared__ uint32_t wsum[NT / 32];
+    constexpr int D = kRadixDigits;
     const int t = threadIdx.x;
     // an odd run length keeps the threads' 64-bit reads a[t * K + i] at most
     // 2-way bank conflicted
     const int K = ((n + NT - 1) / NT) | 1;
     const int i0 = min(n, t * K), i1 = min(n, i0 + K);
-    for (int bit = lo; bit < lo + nbits; bit += 4) {
+    for (int bit = lo; bit < lo + nbits; bit += kRadixBits) {
 #pragma unroll
-        for (int d = 0; d < 16; ++d) hist[hpad(d * NT + t)] = 0;
-        for (int i = i0; i < i1; ++i) hist[hpad((int)((uint32_t)(a[i] >> bit) & 15u) * NT + t)]++;
+        for (int d = 0; d < D; ++d) hist[hpad(d * NT + t)] = 0;
+        for (int i = i0; i < i1; ++i) hist[hpad((int)((uint32_t)(a[i] >> bit) & (D - 1)) * NT + t)]++;
         __syncthreads();
-        // exclusive scan of hist in (digit, thread) order; thread t owns 16 entries
-        uint32_t loc[16], sum = 0;
+        // exclusive scan of hist in (digit, thread) order; thread t owns D entries
+        uint32_t loc[D], sum = 0;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) { loc[q] = hist[17 * t + q]; sum += loc[q]; }
+        for (int q = 0; q < D; ++q) { loc[q] = hist[hpad(D * t + q)]; sum += loc[q]; }
         uint32_t total;
         uint32_t pre = block_excl_scan<NT>(sum, wsum, total);
 #pragma unroll
-        for (int q = 0; q < 16; ++q) { hist[17 * t + q] = pre; pre += loc[q]; }
+        for (int q = 0; q < D; ++q) { hist[hpad(D * t + q)] = pre; pre += loc[q]; }
         __syncthreads();
         for (int i = i0; i < i1; ++i) {
             const uint64_t v = a[i];
-            b[hist[hpad((int)((uint32_t)(v >> bit) & 15u) * NT + t)]++] = v;
+            b[hist[hpad((int)((uint32_t)(v >> bit) & (D - 1)) * NT + t)]++] = v;
         }
         __syncthreads();
         uint64_t *tmp = a; a = b; b = tmp;
@@ -985,10 +990,12 @@ __device__ uint64_t *block_radix_sort(uint64_t *a, uint64_t *b, uint32_t *hist, 
 // inside its bucket by counting the smaller ids there.  Keys whose ids bunch
 // into a few buckets (more than kBucketMax in one) go to the radix sort
 // instead, so the result never depends on the id distribution and the cost
-// never grows quadratically.  NT threads; `cnt` holds kBuckets + 1 words.
+// never grows quadratically.  NT threads; `cnt` holds kRadixWords(NT) >=
+// kBuckets + 1 words.
 // Returns the buffer that holds the sorted keys.
 constexpr int kBuckets = 512;
 constexpr int kBucketMax = 24;
+static_assert(kRadixWords(128) >= kBuckets + 1, "the bucket counters fit the radix table");
 
 template <int NT>
 __device__ uint64_t *block_bucket_sort(uint64_t *a, uint64_t *b, uint32_t *cnt, int n, int id_bits)
@@ -1079,7 +1086,7 @@ constexpr int kMaxCuts = 32;                   // id windows of a huge cell plan
 // separation, alignment) over the id-ordered candidate list; the ordered sums
 // then walk the masks.  kMaskWords words hold the masks of one round of
 // boids, so a round takes at most kMaskWords / (3 * words) boids.
-constexpr int kMaskWords = kDenseCap + 17 * kDT;
+constexpr int kMaskWords = kDenseCap + kRadixWords(kDT);
 // At most kSumsMax boids per round: the per-boid table of the exact tests and
 // the per-boid results of the ordered sums hold that many.
 constexpr int kSumsMax = 85;
@@ -1099,7 +1106,7 @@ struct DenseSmem {
     union {
         struct {
             uint32_t gslot[kDenseCap];      // state slot, by gather index
-            uint32_t hist[17 * kDT];        // radix counters, padded (block_radix_sort)
+            uint32_t hist[kRadixWords(kDT)];  // sort counters (block_bucket_sort, block_radix_sort)
         } s;
         uint32_t masks[kMaskWords];         // rule r of round boid i: words (r * nbr + i) * wstride ...
     } v;
@@ -1242,7 +1249,7 @@ __device__ __forceinline__ void dense_hash_job(const DenseSmem &sm, const uint32
 // running count passes kDenseCap; if the first bin alone is over, the span
 // narrows to that bin.  A boid is a candidate at most once (G >= 3), so a
 // bin one id wide always fits and the search ends.
-constexpr int kWinBins = 2048;
+constexpr int kWinBins = 1536;
 
 __device__ uint32_t dense_window(DenseSmem &sm, const GridIn &g, int ns, uint32_t lo, uint32_t nid)
 {
@@ -1379,7 +1386,7 @@ __device__ void dense_window_plan(DenseSmem &sm, const GridIn &g, int ns, uint32
 // in ascending id windows that each fit the list; the sums are carried from
 // window to window through o.carry.
 template <bool DIAG, bool MULTI>
-__global__ void __launch_bounds__(kDT, 4)
+__global__ void __launch_bounds__(kDT, kDenseCtasPerSm)
 k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint32_t *__restrict__ dense_n,
              StepConst kp, FlockTable ft)
 {

@@ -200,7 +200,7 @@ extern "C" int boids_step_noalloc(const boids_params *params, const float *pos3n
     layout(k, base, &b);
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, params->device);
-    b.dense_grid = (uint32_t)(nsm > 0 ? nsm : 1) * 4;
+    b.dense_grid = (uint32_t)(nsm > 0 ? nsm : 1) * boidsgpu::kDenseCtasPerSm;
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     uint64_t launches = 0;
     // the array keeps the previous call's contents: clear what must start at zero
