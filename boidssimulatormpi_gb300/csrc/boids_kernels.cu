@@ -1089,10 +1089,10 @@ constexpr int kMaxCuts = 32;                   // id windows of a huge cell plan
 constexpr int kMaskWords = kDenseCap + kRadixWords(kDT);
 // At most kSumsMax boids per round: the per-boid table of the exact tests and
 // the per-boid results of the ordered sums hold that many.
-constexpr int kSumsMax = 85;
+constexpr int kSumsMax = 72;
 // Filter hits queued per warp for the exact tests: a filter iteration adds at
 // most two per lane, so the queue is flushed once it holds kQueue - 64.
-constexpr int kQueue = 256;
+constexpr int kQueue = 192;
 
 // Shared memory of k_grid_dense.  Regions whose lifetimes do not overlap
 // share storage: the sort keys become the id-ordered candidate array, the
