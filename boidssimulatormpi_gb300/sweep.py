@@ -128,6 +128,47 @@ def recall(chosen: np.ndarray, truth: np.ndarray) -> float:
     return len(set(chosen.tolist()) & set(truth.tolist())) / max(1, len(truth))
 
 
+# ---------------------------------------------------------------- selection without the network
+#
+# What the same re-simulation budget buys without the surrogate: k sweep
+# points chosen blind to the statistic (at random, or spread over the
+# parameter box by a Latin hypercube), or ranked by a least-squares linear
+# model fitted to the same training runs.
+
+def random_subset(n: int, k: int, seed: int = 0) -> np.ndarray:
+    """k distinct indices of n, uniformly at random."""
+    return np.random.default_rng(seed).choice(n, size=min(k, n), replace=False)
+
+
+def lhs_subset(u: np.ndarray, k: int, seed: int = 0) -> np.ndarray:
+    """k distinct points of u spread over the unit cube: for each point of a
+    fresh k-point Latin hypercube, the nearest point of u not taken yet."""
+    u = np.asarray(u)
+    design = latin_hypercube(min(k, len(u)), u.shape[1], seed=seed)
+    free = np.ones(len(u), bool)
+    out = []
+    for x in design:
+        d = ((u - x) ** 2).sum(1)
+        d[~free] = np.inf
+        i = int(np.argmin(d))
+        free[i] = False
+        out.append(i)
+    return np.array(out, dtype=np.int64)
+
+
+def linear_predict(u_train: np.ndarray, y_train: np.ndarray, u: np.ndarray) -> np.ndarray:
+    """Least-squares affine model of the statistics on the parameters."""
+    a = np.c_[np.asarray(u_train), np.ones(len(u_train))]
+    w, *_ = np.linalg.lstsq(a, np.asarray(y_train), rcond=None)
+    return np.c_[np.asarray(u), np.ones(len(u))] @ w
+
+
+def blind_recalls(us: np.ndarray, truth: np.ndarray, k: int, seed: int = 0) -> dict:
+    """Recall of the true top set by k points chosen without the network."""
+    return {"random": recall(random_subset(len(us), k, seed), truth),
+            "latin_hypercube": recall(lhs_subset(us, k, seed), truth)}
+
+
 def run(n_boids=2048, steps=300, n_train=1024, n_sweep=8192, frac=0.02, oversample=(1, 2, 4), epochs=300,
         seed=12345, noise_points=64):
     """Plain sweep vs surrogate-screened sweep on the same Latin hypercube;
@@ -144,12 +185,14 @@ def run(n_boids=2048, steps=300, n_train=1024, n_sweep=8192, frac=0.02, oversamp
     t0 = time.perf_counter()
     pred = sc.predict(us)
     infer_s = time.perf_counter() - t0
+    lin = linear_predict(ut, st_train, us)
     out = {"n_boids": n_boids, "steps": steps, "train_points": n_train, "sweep_points": n_sweep, "frac": frac,
            "gpu_s": {"train_simulations": gpu_train, "plain_sweep": gpu_plain, "fit": fit_s, "inference": infer_s},
            "fit_loss": loss, "objectives": {}}
     for o, name in enumerate(OBJECTIVES):
         truth = top(st_plain[:, o], frac)
         res = {"corr": float(np.corrcoef(pred[:, o], st_plain[:, o])[0, 1]),
+               "linear_corr": float(np.corrcoef(lin[:, o], st_plain[:, o])[0, 1]),
                "rmse": float(np.sqrt(np.mean((pred[:, o] - st_plain[:, o]) ** 2))),
                "spread": float(st_plain[:, o].std()),
                "seed_noise": float((st_other[:, o] - st_plain[:noise_points, o]).std() / np.sqrt(2)),
@@ -159,7 +202,10 @@ def run(n_boids=2048, steps=300, n_train=1024, n_sweep=8192, frac=0.02, oversamp
             _, sim_s = simulate(us[pick], n_boids, steps, seed)
             res["recall"]["x%d" % m] = {"recall": recall(pick, truth), "resimulated": int(pick.size),
                                         "gpu_s": infer_s + sim_s,
-                                        "fraction_of_plain": (infer_s + sim_s) / gpu_plain}
+                                        "fraction_of_plain": (infer_s + sim_s) / gpu_plain,
+                                        "without_network": dict(blind_recalls(us, truth, pick.size, seed=m),
+                                                                linear_model=recall(top(lin[:, o], frac * m),
+                                                                                    truth))}
         out["objectives"][name] = res
     sc.close()
     return out
@@ -176,5 +222,10 @@ if __name__ == "__main__":
     ap.add_argument("--sweep", type=int, default=8192)
     ap.add_argument("--frac", type=float, default=0.02)
     ap.add_argument("--epochs", type=int, default=300)
+    ap.add_argument("--out", default="", help="also write the record to this file")
     a = ap.parse_args()
-    print(json.dumps(run(a.boids, a.steps, a.train, a.sweep, a.frac, epochs=a.epochs)))
+    rec = run(a.boids, a.steps, a.train, a.sweep, a.frac, epochs=a.epochs)
+    print(json.dumps(rec))
+    if a.out:
+        with open(a.out, "w") as f:
+            json.dump(rec, f, indent=1)

@@ -43,3 +43,23 @@ def test_top_fraction_and_recall():
     assert S.top(vals, 0.01).tolist() == [1]             # at least one
     assert S.recall(np.array([1, 7, 5]), S.top(vals, 0.3)) == pytest.approx(2 / 3)
     assert S.recall(np.array([], dtype=int), np.array([], dtype=int)) == 0.0
+
+
+def test_selection_without_the_network():
+    """The blind subsets the screened sweep is compared with: the requested
+    size, distinct indices, seeded; the Latin-hypercube subset's first pick is
+    the sweep point nearest the design's first point; and the linear model
+    fits an affine function exactly."""
+    from boidssimulatormpi_gb300 import sweep as S
+    us = S.latin_hypercube(400, seed=2)
+    r = S.random_subset(400, 40, seed=3)
+    assert r.size == 40 and np.unique(r).size == 40 and np.array_equal(r, S.random_subset(400, 40, seed=3))
+    l = S.lhs_subset(us, 40, seed=3)
+    assert l.size == 40 and np.unique(l).size == 40 and np.array_equal(l, S.lhs_subset(us, 40, seed=3))
+    d0 = S.latin_hypercube(40, 8, seed=3)[0]
+    assert l[0] == np.argmin(((us - d0) ** 2).sum(1))
+    truth = S.top(us[:, 0], 0.1)
+    b = S.blind_recalls(us, truth, 40, seed=3)
+    assert set(b) == {"random", "latin_hypercube"} and all(0 <= v <= 1 for v in b.values())
+    y = us @ np.arange(1, 9, dtype=float)[:, None] * np.ones((1, 4)) + 0.5
+    assert np.allclose(S.linear_predict(us, y, us[:5]), y[:5])
