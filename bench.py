@@ -25,8 +25,9 @@ timed state against the CPU baseline's, bit for bit), `trajectory` (the
 workload's whole 1000-update run from its seeded initial state, timed as one
 region, with default thresholds and with one retune), `late_regime` (steps
 after that run, when the flock has gathered), `allpairs` (the all-pairs
-engine's N^2 kernels at N=65536, F=1.6, against the FP32 lane-issue peak) and
-`ensemble` (the 256-flock batched sweep).
+engine's N^2 kernels at N=65536, F=1.6, against the FP32 lane-issue peak),
+`ensemble` (the 256-flock batched sweep) and `surrogate_sweep` (the recorded
+plain vs screened sweep at 16 384 boids and 2000 updates, not timed here).
 
 Multi-GPU (torchrun, N > 1): independent replicas, one per GPU, each with its
 own seed; value = boid-steps of all ranks / the slowest rank's time.
@@ -552,6 +553,25 @@ def run_ours(a):
                 roofline["issue"] = tj["issue"]
         except (OSError, ValueError):
             pass
+    # the surrogate-screened sweep at 16 384 boids and 2000 updates is a
+    # 14-minute run of its own (boidssimulatormpi_gb300.sweep); its recorded
+    # result rides along, marked as such
+    sweep_rec = None
+    sw = os.path.join(ROOT, "profiles", "sweep_n16384_t2000.json")
+    if os.path.exists(sw):
+        try:
+            with open(sw) as f:
+                sj = json.load(f)
+            sweep_rec = {"recorded": "profiles/sweep_n16384_t2000.json (not timed in this run)",
+                         "n_boids": sj["n_boids"], "steps": sj["steps"], "sweep_points": sj["sweep_points"],
+                         "train_points": sj["train_points"], "frac": sj["frac"],
+                         "plain_sweep_gpu_s": sj["gpu_s"]["plain_sweep"],
+                         "screened": {o: {m: {"recall": x["recall"], "fraction_of_plain": x["fraction_of_plain"],
+                                              "random_recall": x["without_network"]["random"]}
+                                          for m, x in r["recall"].items()}
+                                      for o, r in sj["objectives"].items()}}
+        except (OSError, ValueError, KeyError):
+            sweep_rec = None
     cpu = None
     if not a.no_cpu_baseline and a.engine == "grid":
         cpu = cpu_baseline_sample(a, pos0.reshape(-1), vel0.reshape(-1), gpu_after)
@@ -563,6 +583,7 @@ def run_ours(a):
             "clocks": clk.summary(),
             "parity": (cpu or {}).get("parity"),
             "trajectory": traj, "late_regime": late, "allpairs": allpairs, "ensemble": ens,
+            "surrogate_sweep": sweep_rec,
             "step_ms_min_max": [min(step_ms), max(step_ms)]}
     print(json.dumps(line), flush=True)
 
