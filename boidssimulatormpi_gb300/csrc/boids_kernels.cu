@@ -1146,32 +1146,30 @@ static_assert(kDenseCap <= 2048, "gather index must fit 11 bits");
 
 // The ordered sums of a round's boids run as jobs, each a (job, boid) pair
 // taken by one lane, job-major so that the lanes of a warp run the same code:
-// job 0 is the cohesion sum (x, y and z, and the count), job 1 the alignment
-// sum, job 2 the separation sum (from the normalised offsets), job 3 the
-// neighbour-set id hashes (diagnostics only).  Each walks its rule's mask word
-// by word from candidate 0 up: ascending id, the reference's order of
-// accumulation, so every float sum is the reference's sequence of additions.
-// One walk feeds the three components' sums, which are independent chains.
-// A job's running values start from the earlier id windows' partial sums
-// (carry) or zero, and end in out.
-__device__ __forceinline__ void dense_sum_job(const DenseSmem &sm, const uint32_t *m, uint32_t words, bool coh,
+// jobs 0-5 are the cohesion sum's x, y, z and the alignment sum's x, y, z
+// (jobs 0 and 3 also count), job 6 the separation sum (all three components,
+// from the normalised offsets), job 7 the neighbour-set id hashes
+// (diagnostics only).  Each walks its rule's mask word by word from candidate
+// 0 up: ascending id, the reference's order of accumulation, so every float
+// sum is the reference's sequence of additions.  A job's running value starts
+// from the earlier id windows' partial sums (carry) or zero, and ends in out.
+__device__ __forceinline__ void dense_sum_job(const DenseSmem &sm, const uint32_t *m, uint32_t words, uint32_t job,
                                               const Acc *carry, Acc &out)
 {
-    float3 acc = carry ? (coh ? carry->coh : carry->ali) : make_float3(0.f, 0.f, 0.f);
-    int cnt = 0;
+    const bool coh = job < 3;
+    const uint32_t c = job % 3;
     // the summands: the candidates' imaged positions, or their velocities
-    auto value = [&](uint32_t q) {
-        if (coh) {
-            const float4 c = sm.u.spos[q];
-            return make_float3(c.x, c.y, c.z);
-        }
-        return make_float3(sm.svx[q], sm.svy[q], sm.svz[q]);
-    };
+    const float *base = coh ? reinterpret_cast<const float *>(sm.u.spos) + c
+                            : (c == 0 ? sm.svx : (c == 1 ? sm.svy : sm.svz));
+    const uint32_t sh = coh ? 2u : 0u;  // element q at base[q << sh]
+    float *dst = reinterpret_cast<float *>(&out) + (coh ? 0 : 6) + c;
+    float acc = carry ? reinterpret_cast<const float *>(carry)[(coh ? 0 : 6) + c] : 0.f;
+    int cnt = 0;
     for (uint32_t w = 0; w < words; ++w) {
         uint32_t bits = m[w];
         cnt += __popc(bits);
         const uint32_t q0 = w * 32;
-        // two entries per iteration: their loads in flight together, their
+        // four entries per iteration: their loads in flight together, their
         // additions in order
         while (bits) {
             const uint32_t b0 = (uint32_t)__ffs(bits) - 1;
@@ -1179,27 +1177,28 @@ __device__ __forceinline__ void dense_sum_job(const DenseSmem &sm, const uint32_
             const bool h1 = bits != 0;
             const uint32_t b1 = h1 ? (uint32_t)__ffs(bits) - 1 : b0;
             bits &= bits - 1;
-            const float3 v0 = value(q0 + b0), v1 = value(q0 + b1);
-            acc.x = __fadd_rn(acc.x, v0.x);
-            acc.y = __fadd_rn(acc.y, v0.y);
-            acc.z = __fadd_rn(acc.z, v0.z);
-            if (h1) {
-                acc.x = __fadd_rn(acc.x, v1.x);
-                acc.y = __fadd_rn(acc.y, v1.y);
-                acc.z = __fadd_rn(acc.z, v1.z);
-            }
+            const bool h2 = bits != 0;
+            const uint32_t b2 = h2 ? (uint32_t)__ffs(bits) - 1 : b0;
+            bits &= bits - 1;
+            const bool h3 = bits != 0;
+            const uint32_t b3 = h3 ? (uint32_t)__ffs(bits) - 1 : b0;
+            bits &= bits - 1;
+            const float v0 = base[(q0 + b0) << sh], v1 = base[(q0 + b1) << sh];
+            const float v2 = base[(q0 + b2) << sh], v3 = base[(q0 + b3) << sh];
+            acc = __fadd_rn(acc, v0);
+            if (h1) acc = __fadd_rn(acc, v1);
+            if (h2) acc = __fadd_rn(acc, v2);
+            if (h3) acc = __fadd_rn(acc, v3);
         }
     }
-    if (coh) {
-        out.coh = acc;
-        out.ncoh = cnt + (carry ? carry->ncoh : 0);
-    } else {
-        out.ali = acc;
-        out.nali = cnt + (carry ? carry->nali : 0);
+    *dst = acc;
+    if (c == 0) {
+        int *n = coh ? &out.ncoh : &out.nali;
+        *n = cnt + (carry ? (coh ? carry->ncoh : carry->nali) : 0);
     }
 }
 
-// Job 2: the separation sum (Vector3D::normalized of pi - t, as acc_add).
+// Job 6: the separation sum (Vector3D::normalized of pi - t, as acc_add).
 __device__ __forceinline__ void dense_sep_job(const DenseSmem &sm, const uint32_t *m, uint32_t words, float3 pi,
                                               const Acc *carry, Acc &out)
 {
@@ -1223,7 +1222,7 @@ __device__ __forceinline__ void dense_sep_job(const DenseSmem &sm, const uint32_
     out.nsep = cnt;
 }
 
-// Job 3 (diagnostics): the order-free id fingerprints of the three sets.
+// Job 7 (diagnostics): the order-free id fingerprints of the three sets.
 __device__ __forceinline__ void dense_hash_job(const DenseSmem &sm, const uint32_t *m0, uint32_t rstride,
                                                uint32_t words, const Acc *carry, Acc &out,
                                                const float4 *__restrict__ pos)
@@ -1542,7 +1541,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
             const uint32_t words = (nw + 31) / 32, wstride = words | 1u;  // odd: boids' words in other banks
             const uint32_t pool_nbr = (uint32_t)kMaskWords / (3u * wstride);
             const uint32_t rend = min(b, rbeg + (uint32_t)kDenseRound);
-            const uint32_t njobs = DIAG ? 4u : 3u;
+            const uint32_t njobs = DIAG ? 8u : 7u;
             for (uint32_t r0 = rbeg; r0 < rend;) {
                 const uint32_t nbr = min(min(rend - r0, (uint32_t)kDT), min((uint32_t)kSumsMax, pool_nbr));
                 const uint32_t L = (uint32_t)kDT / nbr;               // lanes per boid
@@ -1633,9 +1632,9 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                     const uint32_t js = own0 + r0 + jb;
                     const Acc *cin = first ? nullptr : o.carry + js;
                     Acc &out = sm.w.sums[jb];
-                    if (job < 2) {
-                        dense_sum_job(sm, masks + (2 * job * nbr + jb) * wstride, words, job == 0, cin, out);
-                    } else if (job == 2) {
+                    if (job < 6) {
+                        dense_sum_job(sm, masks + ((job < 3 ? 0u : 2u) * nbr + jb) * wstride, words, job, cin, out);
+                    } else if (job == 6) {
                         dense_sep_job(sm, masks + (nbr + jb) * wstride, words, xyz(g.pos[js]), cin, out);
                     } else if (DIAG) {
                         dense_hash_job(sm, masks + jb * wstride, nbr * wstride, words, cin, out, g.pos);
