@@ -771,10 +771,18 @@ __device__ __forceinline__ void sparse_pass(SparseSmem &sm, int t, uint32_t s, f
             if (vc[u]) filter(pc[u], qc[u], cc[u], sc[u]);
         // exact tests of the buffered hits, the whole warp together
         if (__any_sync(0xffffffffu, nb > kBufA - kCandStep) || it + kCandStep >= max_nc) {
+            // each entry's candidate is loaded one entry ahead, so that its
+            // load is in flight while the previous entry is tested
+            uint32_t wb_next = nb > 0 ? sm.buf[0][t] : 0u;
+            float4 pj_next = nb > 0 ? __ldg(g.pos + (wb_next & 0x7fffffffu)) : make_float4(0.f, 0.f, 0.f, 0.f);
             for (int q = 0; q < nb; ++q) {
-                const uint32_t wb = sm.buf[q][t];
+                const uint32_t wb = wb_next;
                 const uint32_t jb = wb & 0x7fffffffu;
-                const float4 pj = __ldg(g.pos + jb);
+                const float4 pj = pj_next;
+                if (q + 1 < nb) {
+                    wb_next = sm.buf[q + 1][t];
+                    pj_next = __ldg(g.pos + (wb_next & 0x7fffffffu));
+                }
                 const uint32_t idj = __float_as_uint(pj.w);
                 if ((int64_t)idj <= lo_id) continue;
                 // a filter hit from a segment without periodic shift is nearer
@@ -795,12 +803,24 @@ __device__ __forceinline__ void sparse_pass(SparseSmem &sm, int t, uint32_t s, f
         }
     }
     if (need) {
+        // the list's neighbours in id order, each loaded one entry ahead
+        uint64_t e_next = m > 0 ? sm.lst[0][t] : 0;
+        float4 p_next = make_float4(0.f, 0.f, 0.f, 0.f), v_next = p_next;
+        if (m > 0) {
+            p_next = __ldg(g.pos + ((uint32_t)e_next & 0x1fffffffu));
+            v_next = __ldg(g.vel + ((uint32_t)e_next & 0x1fffffffu));
+        }
         for (int q = 0; q < m; ++q) {
-            const uint64_t e = sm.lst[q][t];
-            const uint32_t jj = (uint32_t)e & 0x1fffffffu;
+            const uint64_t e = e_next;
+            const float4 pj = p_next, vv = v_next;
+            if (q + 1 < m) {
+                e_next = sm.lst[q + 1][t];
+                p_next = __ldg(g.pos + ((uint32_t)e_next & 0x1fffffffu));
+                v_next = __ldg(g.vel + ((uint32_t)e_next & 0x1fffffffu));
+            }
             const int f = (int)(((uint32_t)e) >> 29);
-            const float3 tt = image3(xyz(__ldg(g.pos + jj)), pi, k);
-            const float3 vj = (f & 4) ? xyz(__ldg(g.vel + jj)) : make_float3(0.f, 0.f, 0.f);
+            const float3 tt = image3(xyz(pj), pi, k);
+            const float3 vj = (f & 4) ? xyz(vv) : make_float3(0.f, 0.f, 0.f);
             acc_add<DIAG>(a, pi, tt, vj, f, (uint32_t)(e >> 32));
         }
         if (more <= (uint32_t)m) need = false;
