@@ -1498,9 +1498,11 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                 __syncthreads();
                 nw = sm.nw;
             } else {
-                // gather every candidate's (id, segment, gather index) key
+                // gather every candidate's (id, segment, gather index) key; a
+                // thread's q only grows, so its segment search goes on from
+                // where the last one stopped
+                uint32_t sgi = 0;
                 for (uint32_t q = t; q < ncand; q += kDT) {
-                    uint32_t sgi = 0;
                     while (q >= sm.seg_k0[sgi + 1]) ++sgi;
                     const uint32_t slot = sm.seg_j0[sgi] + (q - sm.seg_k0[sgi]);
                     sm.v.s.gslot[q] = slot;
@@ -1600,49 +1602,70 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                     const uint32_t p0 = k0 >> 1, plen = k1 > k0 ? ((k1 + 1) >> 1) - p0 : 0;  // pairs
                     const uint32_t maxlen = __reduce_max_sync(0xffffffffu, plen);
                     const int lane = t & 31;
-                    const unsigned below = (1u << lane) - 1u;
                     uint32_t *queue = sm.w.a.queue[t >> 5];
                     uint32_t qlen = 0;  // the same in every lane of the warp
+                    // exact tests of the queued hits, every lane of the warp
+                    // busy; accepted neighbours are marked in the boid's masks
+                    auto flush = [&]() {
+                        __syncwarp();
+                        for (uint32_t e = (uint32_t)lane; e < qlen; e += 32) {
+                            const uint32_t en = queue[e];
+                            const uint32_t eb = en >> 11, q = en & 0x7ffu;
+                            const float4 cq = sm.u.spos[q];
+                            if (__float_as_uint(cq.w) == own0 + r0 + eb) continue;
+                            const float4 a0 = sm.w.a.obs[0][eb], a1 = sm.w.a.obs[1][eb];
+                            Sight sg;
+                            sg.v = xyz(a1);
+                            sg.nv = a0.w;
+                            sg.inv_nv = a1.w;
+                            const int f = pair_flags(xyz(a0), sg, xyz(cq), k);
+                            if (!f) continue;
+                            uint32_t *mb = masks + eb * wstride + (q >> 5);
+                            const uint32_t bit = 1u << (q & 31);
+                            if (f & 1) atomicOr(mb, bit);
+                            if (f & 2) atomicOr(mb + nbr * wstride, bit);
+                            if (f & 4) atomicOr(mb + 2 * nbr * wstride, bit);
+                        }
+                        __syncwarp();
+                        qlen = 0;
+                    };
+                    // A lane's hits of kHitGroup iterations (two candidates
+                    // each) collect in a register, then go to the warp's queue
+                    // together (one scan of the lanes' counts); the queue is
+                    // tested first when they would not fit.
+                    constexpr uint32_t kHitGroup = kQueue / 64;
+                    uint32_t hm = 0;
                     for (uint32_t it = 0; it < maxlen; ++it) {
-                        bool h0 = false, h1 = false;
-                        const uint32_t pp = p0 + it;
+                        const uint32_t gi = it % kHitGroup;
                         if (it < plen) {
+                            const uint32_t pp = p0 + it;
                             const __half2 dx = __hsub2(sm.hx[pp], bx), dy = __hsub2(sm.hy[pp], by),
                                           dz = __hsub2(sm.hz[pp], bz);
                             const __half2 d2 = __hfma2(dz, dz, __hfma2(dy, dy, __hmul2(dx, dx)));
                             const __half2 dv = __hfma2(hvz, dz, __hfma2(hvy, dy, __hmul2(hvx, dx)));
                             const unsigned keep = __hlt2_mask(d2, hf2) & __hge2_mask(dv, hd2);
-                            h0 = (keep & 0xffffu) != 0;
-                            h1 = (keep >> 16) != 0;
+                            hm |= ((keep & 1u) | ((keep >> 15) & 2u)) << (2 * gi);
                         }
-                        const unsigned b0 = __ballot_sync(0xffffffffu, h0), b1 = __ballot_sync(0xffffffffu, h1);
-                        if (h0) queue[qlen + __popc(b0 & below)] = (bi << 11) | (2 * pp);
-                        if (h1) queue[qlen + __popc(b0) + __popc(b1 & below)] = (bi << 11) | (2 * pp + 1);
-                        qlen += __popc(b0) + __popc(b1);
-                        // exact tests of the queued hits, every lane of the warp
-                        // busy; accepted neighbours are marked in the boid's masks
-                        if (qlen > (uint32_t)(kQueue - 64) || it + 1 == maxlen) {
-                            __syncwarp();
-                            for (uint32_t e = (uint32_t)lane; e < qlen; e += 32) {
-                                const uint32_t en = queue[e];
-                                const uint32_t eb = en >> 11, q = en & 0x7ffu;
-                                const float4 cq = sm.u.spos[q];
-                                if (__float_as_uint(cq.w) == own0 + r0 + eb) continue;
-                                const float4 a0 = sm.w.a.obs[0][eb], a1 = sm.w.a.obs[1][eb];
-                                Sight sg;
-                                sg.v = xyz(a1);
-                                sg.nv = a0.w;
-                                sg.inv_nv = a1.w;
-                                const int f = pair_flags(xyz(a0), sg, xyz(cq), k);
-                                if (!f) continue;
-                                uint32_t *mb = masks + eb * wstride + (q >> 5);
-                                const uint32_t bit = 1u << (q & 31);
-                                if (f & 1) atomicOr(mb, bit);
-                                if (f & 2) atomicOr(mb + nbr * wstride, bit);
-                                if (f & 4) atomicOr(mb + 2 * nbr * wstride, bit);
+                        const bool end = it + 1 == maxlen;
+                        if (gi == kHitGroup - 1 || end) {
+                            const uint32_t cnt = __popc(hm);
+                            uint32_t incl = cnt;
+#pragma unroll
+                            for (int o = 1; o < 32; o <<= 1) {
+                                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                                if (lane >= o) incl += y;
                             }
-                            __syncwarp();
-                            qlen = 0;
+                            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                            if (qlen + total > (uint32_t)kQueue) flush();
+                            uint32_t at = qlen + incl - cnt;
+                            const uint32_t q0 = 2 * (p0 + it - gi);  // the candidate of bit 0
+                            while (hm) {
+                                const uint32_t bb = (uint32_t)__ffs(hm) - 1;
+                                hm &= hm - 1;
+                                queue[at++] = (bi << 11) | (q0 + bb);
+                            }
+                            qlen += total;
+                            if (end || qlen > (uint32_t)kQueue - 64) flush();
                         }
                     }
                 }
