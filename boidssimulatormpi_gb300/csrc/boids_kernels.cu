@@ -1185,8 +1185,10 @@ __device__ __forceinline__ void dense_sum_job(const DenseSmem &sm, const uint32_
     float *dst = reinterpret_cast<float *>(&out) + (coh ? 0 : 6) + c;
     float acc = carry ? reinterpret_cast<const float *>(carry)[(coh ? 0 : 6) + c] : 0.f;
     int cnt = 0;
+    uint32_t next = words > 0 ? m[0] : 0u;  // each mask word is read one word ahead
     for (uint32_t w = 0; w < words; ++w) {
-        uint32_t bits = m[w];
+        uint32_t bits = next;
+        if (w + 1 < words) next = m[w + 1];
         cnt += __popc(bits);
         const uint32_t q0 = w * 32;
         // four entries per iteration: their loads in flight together, their
@@ -1224,8 +1226,10 @@ __device__ __forceinline__ void dense_sep_job(const DenseSmem &sm, const uint32_
 {
     float3 sep = carry ? carry->sep : make_float3(0.f, 0.f, 0.f);
     int cnt = carry ? carry->nsep : 0;
+    uint32_t next = words > 0 ? m[0] : 0u;
     for (uint32_t w = 0; w < words; ++w) {
-        uint32_t bits = m[w];
+        uint32_t bits = next;
+        if (w + 1 < words) next = m[w + 1];
         cnt += __popc(bits);
         while (bits) {
             const uint32_t q = w * 32 + (uint32_t)(__ffs(bits) - 1);
@@ -1437,16 +1441,23 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
         const int G = k.G;
         const int cx = (int)(c % G), cy = (int)((c / G) % G), cz = (int)(c / ((uint32_t)G * G));
         const int runs = seg_runs(cx, k), ns = 9 * runs;
-        if (t < ns) {
-            const Seg sg = segment(cx, cy, cz, t, runs, k);
-            sm.seg_j0[t] = slot_start(g.lstart, g.bsum, k.cell_base + sg.c0, k);
-            sm.seg_k0[t + 1] = slot_start(g.lstart, g.bsum, k.cell_base + sg.c1, k) - sm.seg_j0[t];  // length for now
-            sm.seg_s[t][0] = sg.sx; sm.seg_s[t][1] = sg.sy; sm.seg_s[t][2] = sg.sz;
-        }
-        __syncthreads();
-        if (t == 0) {
-            sm.seg_k0[0] = 0;
-            for (int q = 0; q < ns; ++q) sm.seg_k0[q + 1] += sm.seg_k0[q];
+        if (t < 32) {  // the segments, and their starts in the gather order (a warp scan of their lengths)
+            uint32_t len = 0;
+            if (t < ns) {
+                const Seg sg = segment(cx, cy, cz, t, runs, k);
+                const uint32_t j0 = slot_start(g.lstart, g.bsum, k.cell_base + sg.c0, k);
+                len = slot_start(g.lstart, g.bsum, k.cell_base + sg.c1, k) - j0;
+                sm.seg_j0[t] = j0;
+                sm.seg_s[t][0] = sg.sx; sm.seg_s[t][1] = sg.sy; sm.seg_s[t][2] = sg.sz;
+            }
+            uint32_t incl = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (t >= o) incl += y;
+            }
+            if (t < ns) sm.seg_k0[t + 1] = incl;
+            if (t == 0) sm.seg_k0[0] = 0;
         }
         __syncthreads();
         const uint32_t ncand = sm.seg_k0[ns];
@@ -1669,6 +1680,11 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                         }
                     }
                 }
+                // the separation job's boid (at most one per thread): its
+                // position from the round's table, which the sums overwrite
+                float3 sep_pi = make_float3(0.f, 0.f, 0.f);
+                for (uint32_t pj = (uint32_t)t; pj < 7 * nbr; pj += kDT)
+                    if (pj >= 6 * nbr) sep_pi = xyz(sm.w.a.obs[0][pj - 6 * nbr]);
                 __syncthreads();  // the masks are complete; the hit buffers are dead
                 for (uint32_t pj = (uint32_t)t; pj < njobs * nbr; pj += kDT) {
                     const uint32_t job = pj / nbr, jb = pj - job * nbr;
@@ -1678,7 +1694,7 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
                     if (job < 6) {
                         dense_sum_job(sm, masks + ((job < 3 ? 0u : 2u) * nbr + jb) * wstride, words, job, cin, out);
                     } else if (job == 6) {
-                        dense_sep_job(sm, masks + (nbr + jb) * wstride, words, xyz(g.pos[js]), cin, out);
+                        dense_sep_job(sm, masks + (nbr + jb) * wstride, words, sep_pi, cin, out);
                     } else if (DIAG) {
                         dense_hash_job(sm, masks + jb * wstride, nbr * wstride, words, cin, out, g.pos);
                     }
