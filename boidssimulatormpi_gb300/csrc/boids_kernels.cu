@@ -1721,30 +1721,53 @@ k_grid_dense(GridIn g, GridOut o, const uint32_t *__restrict__ dense_list, uint3
 // Phase 1: a 2-D grid of (i-tile, j-tile) blocks tests every ordered pair.
 // A box filter on the minimum-image offset (||dx| - F/2| > F/2 - R per axis)
 // rejects almost all pairs; survivors get the exact tests and accepted
-// neighbours are appended to the boid's list (unordered).
+// neighbours are appended to the boid's list (unordered).  A thread's box
+// hits are buffered and the whole warp runs their exact tests together once a
+// buffer is nearly full (and at the end of the tile), so the rare hits do not
+// stall the filter loop of the other 31 lanes, as they would inline.
 constexpr int kApThreads = 128;
 constexpr int kApKI = 8;                        // i per thread
 constexpr int kApTileI = kApThreads * kApKI;    // 1024
 constexpr int kApTileJ = 1024;
+constexpr int kApHits = 24;                     // box hits buffered per thread
+static_assert(kApHits > kApKI, "a j step's hits fit the buffer");
 
 __global__ void __launch_bounds__(kApThreads)
 k_ap_pairs(const float4 *__restrict__ pos, const float4 *__restrict__ vel, uint32_t *__restrict__ cnt,
            uint32_t *__restrict__ list, uint32_t cap, StepConst k)
 {
     __shared__ float4 sp[kApTileJ];
+    __shared__ uint16_t hits[kApHits][kApThreads];  // r << 10 | tile j
     const uint32_t n = k.n;
     const uint32_t j0 = blockIdx.y * kApTileJ;
     const uint32_t jn = min((uint32_t)kApTileJ, n - j0);
+    const uint32_t ibase = blockIdx.x * kApTileI + threadIdx.x;
     for (uint32_t t = threadIdx.x; t < jn; t += kApThreads) sp[t] = pos[j0 + t];
     float3 pi[kApKI];
-    uint32_t ii[kApKI];
     const float nanf_ = __uint_as_float(0x7fffffffu);  // fails every filter test
 #pragma unroll
     for (int r = 0; r < kApKI; ++r) {
-        ii[r] = blockIdx.x * kApTileI + r * kApThreads + threadIdx.x;
-        pi[r] = ii[r] < n ? xyz(pos[ii[r]]) : make_float3(nanf_, nanf_, nanf_);
+        const uint32_t i = ibase + r * kApThreads;
+        pi[r] = i < n ? xyz(pos[i]) : make_float3(nanf_, nanf_, nanf_);
     }
     __syncthreads();
+    int nh = 0;
+    // the exact tests of this thread's buffered hits (all lanes call it)
+    auto flush = [&]() {
+        for (int e = 0; e < nh; ++e) {
+            const uint32_t en = hits[e][threadIdx.x];
+            const uint32_t i = ibase + (en >> 10) * kApThreads, tj = en & 1023u, j = j0 + tj;
+            if (i == j) continue;
+            const float3 p = xyz(pos[i]);
+            const Sight s = make_sight(xyz(vel[i]));
+            const int f = pair_flags(p, s, image3(xyz(sp[tj]), p, k), k);
+            if (f) {
+                const uint32_t q = atomicAdd(cnt + i, 1u);
+                if (q < cap) list[(size_t)i * cap + q] = j | ((uint32_t)f << 29);
+            }
+        }
+        nh = 0;
+    };
     const float h = k.halfFf, lim = k.box_lim;
     for (uint32_t t = 0; t < jn; ++t) {
         const float4 pj = sp[t];
@@ -1753,18 +1776,11 @@ k_ap_pairs(const float4 *__restrict__ pos, const float4 *__restrict__ vel, uint3
             const bool nx = fabsf(fabsf(pj.x - pi[r].x) - h) > lim;
             const bool ny = fabsf(fabsf(pj.y - pi[r].y) - h) > lim;
             const bool nz = fabsf(fabsf(pj.z - pi[r].z) - h) > lim;
-            if (nx && ny && nz) {
-                const uint32_t i = ii[r], j = j0 + t;
-                if (i == j) continue;
-                const Sight s = make_sight(xyz(vel[i]));
-                const int f = pair_flags(pi[r], s, image3(xyz(pj), pi[r], k), k);
-                if (f) {
-                    const uint32_t q = atomicAdd(cnt + i, 1u);
-                    if (q < cap) list[(size_t)i * cap + q] = j | ((uint32_t)f << 29);
-                }
-            }
+            if (nx && ny && nz) hits[nh++][threadIdx.x] = (uint16_t)((r << 10) | t);
         }
+        if (__any_sync(0xffffffffu, nh > kApHits - kApKI)) flush();
     }
+    flush();
 }
 
 // Phase 2: per boid, sort its neighbours by id and accumulate in that order,

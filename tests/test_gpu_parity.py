@@ -340,7 +340,7 @@ def test_allpairs_engine_kernel_choice(boids_lib, oracle_mod):
             q[:40, 0] += np.float32(field)      # beyond the far face
             q[40:80, 1] -= np.float32(0.25)     # below zero
         sim.set_state(q, vel)
-        assert sim.grid_info()["list_capacity"] == (64 if outside else 12)
+        assert sim.grid_info()["list_capacity"] == (256 if outside else 12)
         sim.update(3)
         op, ov, of = _oracle_run(O, p, "allpairs", q.reshape(-1), vel.reshape(-1), 3)
         gp, gv = sim.state()
