@@ -7,11 +7,17 @@
 // parameter sweep can be screened before the plain simulation re-runs the
 // candidates it selects.  No counterpart in the reference.
 //
-// Every product -- forward, the input gradient and the weight gradient of
-// the backward pass -- is one strided GEMM kernel on mma.sync m16n8k16
-// (BF16 operands, FP32 accumulators): the layer widths (8, 256, 4) make
-// these small, latency-bound products, where a warp-level MMA with operands
-// read straight from L2 is the simplest fast form.
+// The forward pass's hidden-to-hidden product (rows x 256 by 256 x 256, the
+// network's one square product) runs on the 5th-generation tensor cores:
+// k_mlp_hidden_tc stages a 128-row tile of the activations and the whole
+// weight matrix in shared memory in the canonical K-major layout, one thread
+// issues tcgen05.mma (M 128, N 256, K 16) into an FP32 accumulator in tensor
+// memory, and the epilogue reads it back with tcgen05.ld, adds the bias and
+// writes the FP32 pre-activation and the BF16 ReLU.  The other products --
+// the thin input and output layers (K or N of 8 and 4) and the backward
+// pass -- are one strided GEMM kernel on mma.sync m16n8k16 (BF16 operands,
+// FP32 accumulators): small, latency-bound products where a warp-level MMA
+// with operands read straight from L2 is the simplest fast form.
 #include "boids.h"
 
 #include <cuda_bf16.h>
@@ -94,6 +100,153 @@ k_mlp_gemm(MatB A, MatB B, float *__restrict__ C, int ldc, __nv_bfloat16 *__rest
             if (C) C[(long long)r * ldc + c] = v;
             if (C16) C16[(long long)r * ld16 + c] = __float2bfloat16_rn(relu16 ? fmaxf(v, 0.f) : v);
         }
+    }
+}
+
+// ------------------------------------------------------------------ hidden layer on tcgen05
+
+// C = A W + b for A rows x 256 (BF16, row-major), W 256 x 256 (BF16, fan-in
+// rows), C to FP32 (pre) and BF16 ReLU (h); 128 rows per CTA.
+//
+// Shared memory holds both operands K-major in 8 x 16-byte core matrices
+// (8 rows of 8 consecutive K elements, 128 bytes): element (r, k) at
+// ((r / 8) * 32 + k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2, so core matrices
+// adjacent along K are 128 bytes apart (the descriptor's leading byte offset)
+// and 8-row groups 4096 bytes apart (its stride byte offset).  The weights
+// arrive already in that layout, transposed (row n of the image holds
+// column n of W), from k_mlp_tile_w.
+constexpr int kTcM = 128, kTcN = 256, kTcK = 256;
+constexpr int kTcThreads = 128;
+constexpr uint32_t kTcABytes = kTcM * kTcK * 2;   // 64 KB
+constexpr uint32_t kTcBBytes = kTcN * kTcK * 2;   // 128 KB
+constexpr size_t kTcSmem = kTcABytes + kTcBBytes + 1024 + 64;
+constexpr uint32_t kTcSpinLimit = 1u << 22;      // bounded wait on the accumulator
+
+__device__ uint32_t g_mlp_tc_error;  // set when a tile's wait gave up (the host reports it)
+
+__host__ __device__ constexpr uint32_t core_off(uint32_t r, uint32_t k)
+{
+    return ((r >> 3) * (kTcK / 8) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+// The weight image: W (K x N, row-major, fan-in rows) as N rows of K, in the
+// core-matrix layout above, one 16-byte row chunk per thread.
+__global__ void k_mlp_tile_w(const __nv_bfloat16 *__restrict__ w, __nv_bfloat16 *__restrict__ img)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;  // chunk: (n, k8)
+    if (i >= (uint32_t)(kTcN * kTcK / 8)) return;
+    const uint32_t n = i / (kTcK / 8), k0 = (i % (kTcK / 8)) * 8;
+    __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) v[e] = w[(size_t)(k0 + e) * kTcN + n];
+    *reinterpret_cast<uint4 *>(reinterpret_cast<unsigned char *>(img) + core_off(n, k0)) =
+        *reinterpret_cast<const uint4 *>(v);
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    // start address, leading and stride byte offsets (all >> 4), the
+    // descriptor version (0b001 at bit 46), no swizzle
+    return (uint64_t)((saddr >> 4) & 0x3fffu) | ((uint64_t)((lbo >> 4) & 0x3fffu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_mlp_hidden_tc(const __nv_bfloat16 *__restrict__ a, int rows, const __nv_bfloat16 *__restrict__ wimg,
+                const float *__restrict__ bias, float *__restrict__ pre, __nv_bfloat16 *__restrict__ h)
+{
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    unsigned char *sa = tc_smem, *sb = tc_smem + kTcABytes;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(tc_smem + kTcABytes + kTcBBytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tc_smem + kTcABytes + kTcBBytes + 8);
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int m0 = blockIdx.x * kTcM;
+    // operands into shared memory (16-byte chunks; rows past the end are zero)
+    for (uint32_t i = t; i < (uint32_t)(kTcM * kTcK / 8); i += kTcThreads) {
+        const uint32_t r = i / (kTcK / 8), k0 = (i % (kTcK / 8)) * 8;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (m0 + (int)r < rows) v = *reinterpret_cast<const uint4 *>(a + (size_t)(m0 + r) * kTcK + k0);
+        *reinterpret_cast<uint4 *>(sa + core_off(r, k0)) = v;
+    }
+    for (uint32_t i = t; i < kTcBBytes / 16; i += kTcThreads)
+        reinterpret_cast<uint4 *>(sb)[i] = reinterpret_cast<const uint4 *>(wimg)[i];
+    const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(mbar);
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {  // the accumulator: 256 columns of tensor memory
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::
+                         "r"((uint32_t)__cvta_generic_to_shared(tmem_slot)), "r"((uint32_t)kTcN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    // the generic-proxy stores above become visible to the tensor cores
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    if (t == 0) {
+        // kind::f16: FP32 D (bit 4), BF16 A and B (bits 7, 10), both K-major,
+        // N / 8 at bit 17, M / 16 at bit 24
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                               ((uint32_t)(kTcM >> 4) << 24);
+        const uint32_t a_s = (uint32_t)__cvta_generic_to_shared(sa), b_s = (uint32_t)__cvta_generic_to_shared(sb);
+#pragma unroll 1
+        for (int kk = 0; kk < kTcK / 16; ++kk) {
+            const uint64_t ad = smem_desc(a_s + kk * 256, 128, (kTcK / 8) * 128);
+            const uint64_t bd = smem_desc(b_s + kk * 256, 128, (kTcK / 8) * 128);
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(kk));
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_a)
+                     : "memory");
+    }
+    // wait for the accumulator (bounded: a wait that gives up flags an error)
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < kTcSpinLimit && !done; ++it)
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(mbar_a)
+                     : "memory");
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!done) {
+        atomicExch(&g_mlp_tc_error, 1u);
+    } else {
+        // epilogue: warp w reads tensor-memory lanes 32w.. (its rows), 8 columns at a time
+        const int r = m0 + warp * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+        for (int c = 0; c < kTcN; c += 8) {
+            uint32_t v[8];
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                           "=r"(v[7])
+                         : "r"(trow + (uint32_t)c));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (r < rows) {
+                float f[8];
+                __align__(16) __nv_bfloat16 hb[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    f[e] = __uint_as_float(v[e]) + bias[c + e];
+                    hb[e] = __float2bfloat16_rn(fmaxf(f[e], 0.f));
+                }
+                float4 *po = reinterpret_cast<float4 *>(pre + (size_t)r * kTcN + c);
+                po[0] = make_float4(f[0], f[1], f[2], f[3]);
+                po[1] = make_float4(f[4], f[5], f[6], f[7]);
+                *reinterpret_cast<uint4 *>(h + (size_t)r * kTcN + c) = *reinterpret_cast<const uint4 *>(hb);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)kTcN));
     }
 }
 
@@ -199,6 +352,7 @@ struct boids_mlp {
     __nv_bfloat16 *x16 = nullptr, *h1 = nullptr, *h2 = nullptr, *dy16 = nullptr, *d2_16 = nullptr, *d1_16 = nullptr;
     double *loss = nullptr;
     cudaStream_t st = nullptr;
+    __nv_bfloat16 *w2img = nullptr;  // the hidden weights in the tensor-core layout (hidden width 256)
 };
 
 namespace {
@@ -245,13 +399,20 @@ MatB transposed(const __nv_bfloat16 *p, int rows, int cols)  // the transpose of
     return MatB{p, 1, rows == 0 ? 0 : cols, cols, rows};
 }
 
-// Forward pass of `rows` rows already in m->x16; output in m->y.
+// Forward pass of `rows` rows already in m->x16; output in m->y.  A hidden
+// width of 256 puts the hidden-to-hidden product on the tensor cores.
 void forward(boids_mlp *m, int rows)
 {
     const __nv_bfloat16 *W1 = m->p16 + m->off[0], *W2 = m->p16 + m->off[2], *W3 = m->p16 + m->off[4];
     const float *b1 = m->p + m->off[1], *b2 = m->p + m->off[3], *b3 = m->p + m->off[5];
     gemm(m, rowmajor(m->x16, rows, m->in), rowmajor(W1, m->in, m->h), m->pre1, m->h, m->h1, m->h, b1, nullptr, 0, 1);
-    gemm(m, rowmajor(m->h1, rows, m->h), rowmajor(W2, m->h, m->h), m->pre2, m->h, m->h2, m->h, b2, nullptr, 0, 1);
+    if (m->w2img) {
+        k_mlp_tile_w<<<nb(kTcN * kTcK / 8, 256), 256, 0, m->st>>>(W2, m->w2img);
+        k_mlp_hidden_tc<<<nb(rows, kTcM), kTcThreads, kTcSmem, m->st>>>(m->h1, rows, m->w2img, b2, m->pre2, m->h2);
+    } else {
+        gemm(m, rowmajor(m->h1, rows, m->h), rowmajor(W2, m->h, m->h), m->pre2, m->h, m->h2, m->h, b2, nullptr, 0,
+             1);
+    }
     gemm(m, rowmajor(m->h2, rows, m->h), rowmajor(W3, m->h, m->out), m->y, m->out, nullptr, 0, b3, nullptr, 0, 0);
 }
 
@@ -279,6 +440,20 @@ void backward(boids_mlp *m, int rows)
     gemm(m, transposed(m->x16, rows, m->in), rowmajor(m->d1_16, rows, m->h), gW1, m->h, nullptr, 0, nullptr, nullptr,
          0, 0);
     k_mlp_colsum<<<m->h, 256, 0, m->st>>>(m->d1, rows, m->h, gb1);
+}
+
+// A tensor-core tile whose wait on its accumulator gave up (the flag is
+// cleared for the next call).
+int tc_status(boids_mlp *m)
+{
+    if (!m->w2img) return 0;
+    uint32_t err = 0;
+    MCK(cudaMemcpyFromSymbolAsync(&err, g_mlp_tc_error, sizeof err, 0, cudaMemcpyDeviceToHost, m->st));
+    MCK(cudaStreamSynchronize(m->st));
+    if (!err) return 0;
+    const uint32_t zero = 0;
+    MCK(cudaMemcpyToSymbolAsync(g_mlp_tc_error, &zero, sizeof zero, 0, cudaMemcpyHostToDevice, m->st));
+    return fail(BOIDS_ECUDA, "boids_mlp: a tensor-core tile's wait for its accumulator gave up");
 }
 
 int upload_rows(boids_mlp *m, const float *x, const float *t, int rows)
@@ -339,6 +514,11 @@ int boids_mlp_create(int32_t n_in, int32_t n_hidden, int32_t n_out, uint64_t see
         k_to_bf16<<<nb(m->np, 256), 256, 0, m->st>>>(m->p, m->p16, m->np);
         ok = cudaStreamSynchronize(m->st) == cudaSuccess;
     }
+    if (ok && n_hidden == kTcN) {  // the hidden product on the tensor cores
+        ok = cudaMalloc(&m->w2img, kTcBBytes) == cudaSuccess &&
+             cudaFuncSetAttribute(k_mlp_hidden_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem) ==
+                 cudaSuccess;
+    }
     if (!ok) {
         cudaGetLastError();
         boids_mlp_destroy(m);
@@ -354,7 +534,7 @@ void boids_mlp_destroy(boids_mlp *m)
     cudaSetDevice(m->device);
     if (m->st) cudaStreamSynchronize(m->st);
     free_acts(m);
-    void *q[] = {m->p, m->grad, m->m, m->v, m->p16, m->loss};
+    void *q[] = {m->p, m->grad, m->m, m->v, m->p16, m->loss, m->w2img};
     for (void *p : q)
         if (p) cudaFree(p);
     if (m->st) cudaStreamDestroy(m->st);
@@ -396,7 +576,7 @@ int boids_mlp_forward(boids_mlp *m, const float *x, int32_t rows, float *y)
     MCK(cudaGetLastError());
     MCK(cudaMemcpyAsync(y, m->y, sizeof(float) * (size_t)rows * m->out, cudaMemcpyDeviceToHost, m->st));
     MCK(cudaStreamSynchronize(m->st));
-    return BOIDS_OK;
+    return tc_status(m);
 }
 
 int boids_mlp_gradient(boids_mlp *m, const float *x, const float *t, int32_t rows, float *grad, double *loss)
@@ -414,7 +594,7 @@ int boids_mlp_gradient(boids_mlp *m, const float *x, const float *t, int32_t row
     MCK(cudaMemcpyAsync(&l, m->loss, 8, cudaMemcpyDeviceToHost, m->st));
     MCK(cudaStreamSynchronize(m->st));
     if (loss) *loss = l;
-    return BOIDS_OK;
+    return tc_status(m);
 }
 
 int boids_mlp_train(boids_mlp *m, const float *x, const float *t, int32_t rows, int32_t epochs, int32_t batch,
@@ -488,6 +668,7 @@ int boids_mlp_train(boids_mlp *m, const float *x, const float *t, int32_t rows, 
         epoch_loss = l / nbatch;
     }
     if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(BOIDS_ECUDA, "boids_mlp_train: kernel launch failed");
+    if (!rc) rc = tc_status(m);
     cudaFree(d_idx);
     cudaFree(bx);
     cudaFree(bt);
