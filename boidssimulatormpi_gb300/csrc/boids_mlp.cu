@@ -151,6 +151,16 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
            ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
 }
 
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, uint32_t src_bytes)
+{
+    // 16 bytes global -> shared without staging in registers; src_bytes 0
+    // fills the destination with zeros
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+
+// One CTA per SM walks 128-row tiles: the weight image is loaded once, and
+// the next tile's activations are copied in (cp.async) while the current
+// tile's accumulator is read out.
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_mlp_hidden_tc(const __nv_bfloat16 *__restrict__ a, int rows, const __nv_bfloat16 *__restrict__ wimg,
                 const float *__restrict__ bias, float *__restrict__ pre, __nv_bfloat16 *__restrict__ h)
@@ -160,16 +170,19 @@ k_mlp_hidden_tc(const __nv_bfloat16 *__restrict__ a, int rows, const __nv_bfloat
     uint64_t *mbar = reinterpret_cast<uint64_t *>(tc_smem + kTcABytes + kTcBBytes);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tc_smem + kTcABytes + kTcBBytes + 8);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int m0 = blockIdx.x * kTcM;
-    // operands into shared memory (16-byte chunks; rows past the end are zero)
-    for (uint32_t i = t; i < (uint32_t)(kTcM * kTcK / 8); i += kTcThreads) {
-        const uint32_t r = i / (kTcK / 8), k0 = (i % (kTcK / 8)) * 8;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (m0 + (int)r < rows) v = *reinterpret_cast<const uint4 *>(a + (size_t)(m0 + r) * kTcK + k0);
-        *reinterpret_cast<uint4 *>(sa + core_off(r, k0)) = v;
-    }
-    for (uint32_t i = t; i < kTcBBytes / 16; i += kTcThreads)
-        reinterpret_cast<uint4 *>(sb)[i] = reinterpret_cast<const uint4 *>(wimg)[i];
+    const int ntiles = (rows + kTcM - 1) / kTcM;
+    const uint32_t sa_s = (uint32_t)__cvta_generic_to_shared(sa), sb_s = (uint32_t)__cvta_generic_to_shared(sb);
+    // a tile's activations into shared memory (rows past the end are zero)
+    auto load_a = [&](int tile) {
+        const int m0 = tile * kTcM;
+        for (uint32_t i = t; i < (uint32_t)(kTcM * kTcK / 8); i += kTcThreads) {
+            const uint32_t r = i / (kTcK / 8), k0 = (i % (kTcK / 8)) * 8;
+            const bool in = m0 + (int)r < rows;
+            cp_async16(sa_s + core_off(r, k0), a + (size_t)(in ? m0 + r : 0) * kTcK + k0, in ? 16u : 0u);
+        }
+    };
+    for (uint32_t i = t; i < kTcBBytes / 16; i += kTcThreads) cp_async16(sb_s + 16 * i, wimg + 8 * i, 16u);
+    if ((int)blockIdx.x < ntiles) load_a(blockIdx.x);
     const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(mbar);
     if (t == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a));
@@ -181,67 +194,94 @@ k_mlp_hidden_tc(const __nv_bfloat16 *__restrict__ a, int rows, const __nv_bfloat
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
-    // the generic-proxy stores above become visible to the tensor cores
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    // the shared-memory writes become visible to the tensor cores
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    if (t == 0) {
-        // kind::f16: FP32 D (bit 4), BF16 A and B (bits 7, 10), both K-major,
-        // N / 8 at bit 17, M / 16 at bit 24
-        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
-                               ((uint32_t)(kTcM >> 4) << 24);
-        const uint32_t a_s = (uint32_t)__cvta_generic_to_shared(sa), b_s = (uint32_t)__cvta_generic_to_shared(sb);
+    // kind::f16: FP32 D (bit 4), BF16 A and B (bits 7, 10), both K-major,
+    // N / 8 at bit 17, M / 16 at bit 24
+    const uint32_t idesc =
+        (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        if (t == 0) {
 #pragma unroll 1
-        for (int kk = 0; kk < kTcK / 16; ++kk) {
-            const uint64_t ad = smem_desc(a_s + kk * 256, 128, (kTcK / 8) * 128);
-            const uint64_t bd = smem_desc(b_s + kk * 256, 128, (kTcK / 8) * 128);
-            asm volatile(
-                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                "l"(ad), "l"(bd), "r"(idesc), "r"(kk));
+            for (int kk = 0; kk < kTcK / 16; ++kk) {
+                const uint64_t ad = smem_desc(sa_s + kk * 256, 128, (kTcK / 8) * 128);
+                const uint64_t bd = smem_desc(sb_s + kk * 256, 128, (kTcK / 8) * 128);
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(kk));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_a)
+                         : "memory");
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_a)
-                     : "memory");
-    }
-    // wait for the accumulator (bounded: a wait that gives up flags an error)
-    uint32_t done = 0;
-    for (uint32_t it = 0; it < kTcSpinLimit && !done; ++it)
-        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
-                     " selp.u32 %0, 1, 0, p;\n}\n"
-                     : "=r"(done)
-                     : "r"(mbar_a)
-                     : "memory");
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (!done) {
-        atomicExch(&g_mlp_tc_error, 1u);
-    } else {
-        // epilogue: warp w reads tensor-memory lanes 32w.. (its rows), 8 columns at a time
-        const int r = m0 + warp * 32 + lane;
+        // wait for the accumulator (bounded: a wait that gives up flags an error)
+        uint32_t done = 0;
+        for (uint32_t it = 0; it < kTcSpinLimit && !done; ++it)
+            asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                         " selp.u32 %0, 1, 0, p;\n}\n"
+                         : "=r"(done)
+                         : "r"(mbar_a), "r"(phase)
+                         : "memory");
+        phase ^= 1u;
+        done = __syncthreads_and(done);  // one decision for the whole CTA
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (!done) {
+            atomicExch(&g_mlp_tc_error, 1u);
+            ok = false;
+            break;
+        }
+        // the activations' buffer is free: the next tile's copy runs under the epilogue
+        const int nxt = tile + gridDim.x;
+        if (nxt < ntiles) load_a(nxt);
+        // epilogue: warp w reads tensor-memory lanes 32w.. (its rows), 32 columns at a time
+        const int r = tile * kTcM + warp * 32 + lane;
         const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
-        for (int c = 0; c < kTcN; c += 8) {
-            uint32_t v[8];
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-                           "=r"(v[7])
-                         : "r"(trow + (uint32_t)c));
+        for (int c = 0; c < kTcN; c += 32) {
+            uint32_t v[32];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                : "r"(trow + (uint32_t)c));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (r < rows) {
-                float f[8];
-                __align__(16) __nv_bfloat16 hb[8];
 #pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    f[e] = __uint_as_float(v[e]) + bias[c + e];
-                    hb[e] = __float2bfloat16_rn(fmaxf(f[e], 0.f));
+                for (int q = 0; q < 32; q += 8) {
+                    float f[8];
+                    __align__(16) __nv_bfloat16 hb[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        f[e] = __uint_as_float(v[q + e]) + __ldg(bias + c + q + e);
+                        hb[e] = __float2bfloat16_rn(fmaxf(f[e], 0.f));
+                    }
+                    if (pre) {
+                        float4 *po = reinterpret_cast<float4 *>(pre + (size_t)r * kTcN + c + q);
+                        po[0] = make_float4(f[0], f[1], f[2], f[3]);
+                        po[1] = make_float4(f[4], f[5], f[6], f[7]);
+                    }
+                    *reinterpret_cast<uint4 *>(h + (size_t)r * kTcN + c + q) = *reinterpret_cast<const uint4 *>(hb);
                 }
-                float4 *po = reinterpret_cast<float4 *>(pre + (size_t)r * kTcN + c);
-                po[0] = make_float4(f[0], f[1], f[2], f[3]);
-                po[1] = make_float4(f[4], f[5], f[6], f[7]);
-                *reinterpret_cast<uint4 *>(h + (size_t)r * kTcN + c) = *reinterpret_cast<const uint4 *>(hb);
             }
         }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();  // the accumulator is read and the next activations are in place
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
+    (void)ok;
+    asm volatile("cp.async.wait_all;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
@@ -353,6 +393,7 @@ struct boids_mlp {
     double *loss = nullptr;
     cudaStream_t st = nullptr;
     __nv_bfloat16 *w2img = nullptr;  // the hidden weights in the tensor-core layout (hidden width 256)
+    unsigned nsm = 1;                 // SMs: the tensor-core kernel's persistent grid
 };
 
 namespace {
@@ -401,14 +442,16 @@ MatB transposed(const __nv_bfloat16 *p, int rows, int cols)  // the transpose of
 
 // Forward pass of `rows` rows already in m->x16; output in m->y.  A hidden
 // width of 256 puts the hidden-to-hidden product on the tensor cores.
-void forward(boids_mlp *m, int rows)
+void forward(boids_mlp *m, int rows, bool need_pre = true)
 {
     const __nv_bfloat16 *W1 = m->p16 + m->off[0], *W2 = m->p16 + m->off[2], *W3 = m->p16 + m->off[4];
     const float *b1 = m->p + m->off[1], *b2 = m->p + m->off[3], *b3 = m->p + m->off[5];
     gemm(m, rowmajor(m->x16, rows, m->in), rowmajor(W1, m->in, m->h), m->pre1, m->h, m->h1, m->h, b1, nullptr, 0, 1);
     if (m->w2img) {
         k_mlp_tile_w<<<nb(kTcN * kTcK / 8, 256), 256, 0, m->st>>>(W2, m->w2img);
-        k_mlp_hidden_tc<<<nb(rows, kTcM), kTcThreads, kTcSmem, m->st>>>(m->h1, rows, m->w2img, b2, m->pre2, m->h2);
+        const unsigned tiles = nb(rows, kTcM);
+        k_mlp_hidden_tc<<<tiles < m->nsm ? tiles : m->nsm, kTcThreads, kTcSmem, m->st>>>(
+            m->h1, rows, m->w2img, b2, need_pre ? m->pre2 : nullptr, m->h2);
     } else {
         gemm(m, rowmajor(m->h1, rows, m->h), rowmajor(W2, m->h, m->h), m->pre2, m->h, m->h2, m->h, b2, nullptr, 0,
              1);
@@ -514,6 +557,9 @@ int boids_mlp_create(int32_t n_in, int32_t n_hidden, int32_t n_out, uint64_t see
         k_to_bf16<<<nb(m->np, 256), 256, 0, m->st>>>(m->p, m->p16, m->np);
         ok = cudaStreamSynchronize(m->st) == cudaSuccess;
     }
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && nsm > 0)
+        m->nsm = (unsigned)nsm;
     if (ok && n_hidden == kTcN) {  // the hidden product on the tensor cores
         ok = cudaMalloc(&m->w2img, kTcBBytes) == cudaSuccess &&
              cudaFuncSetAttribute(k_mlp_hidden_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem) ==
@@ -572,7 +618,7 @@ int boids_mlp_forward(boids_mlp *m, const float *x, int32_t rows, float *y)
     cudaSetDevice(m->device);
     if (int rc = ensure_rows(m, rows)) return rc;
     if (int rc = upload_rows(m, x, nullptr, rows)) return rc;
-    forward(m, rows);
+    forward(m, rows, false);  // inference: the backward pass's pre-activations are not needed
     MCK(cudaGetLastError());
     MCK(cudaMemcpyAsync(y, m->y, sizeof(float) * (size_t)rows * m->out, cudaMemcpyDeviceToHost, m->st));
     MCK(cudaStreamSynchronize(m->st));
