@@ -290,6 +290,198 @@ k_mlp_hidden_tc(const __nv_bfloat16 *__restrict__ a, int rows, const __nv_bfloat
     }
 }
 
+// The whole forward pass for inference, fused: 8 -> 256 -> 256 -> 4 in one
+// kernel that reads x and writes y.  Per 128-row tile the CTA computes the
+// first layer into shared memory (each lane keeps its 8 columns of W1 in
+// registers; the tile's x is copied in ahead with cp.async), the tensor
+// cores run the hidden product into one of two accumulators in tensor
+// memory, and the epilogue applies bias and ReLU and folds the 256 -> 4
+// output layer in registers while the next tile's product runs in the other
+// accumulator.  Eight warps: warps w and w + 4 read the same accumulator
+// lanes, the first the columns 0..127, the second 128..255, and their partial
+// outputs meet in shared memory.  The rounding points are those of the
+// unfused pass (BF16 x, h1, h2; FP32 sums).
+constexpr int kTcIn = 8, kTcOut = 4;
+constexpr int kTcFwdThreads = 256;
+constexpr uint32_t kTcXBytes = kTcM * kTcIn * 4;  // a tile's inputs, 4 KB
+constexpr size_t kTcFwdSmem = kTcABytes + kTcBBytes + 1024 + 64 +
+                              sizeof(float) * (kTcN * kTcOut + kTcN + kTcOut + 2 * kTcM * kTcOut) + kTcXBytes;
+
+__global__ void __launch_bounds__(kTcFwdThreads, 1)
+k_mlp_forward_tc(const float *__restrict__ x, int rows, const __nv_bfloat16 *__restrict__ w1,
+                 const float *__restrict__ b1, const __nv_bfloat16 *__restrict__ wimg, const float *__restrict__ b2,
+                 const __nv_bfloat16 *__restrict__ w3, const float *__restrict__ b3, float *__restrict__ y)
+{
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    unsigned char *sa = tc_smem, *sb = tc_smem + kTcABytes;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(tc_smem + kTcABytes + kTcBBytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tc_smem + kTcABytes + kTcBBytes + 8);
+    float *sw3 = reinterpret_cast<float *>(tc_smem + kTcABytes + kTcBBytes + 64);  // W3 as float, [k][j]
+    float *sb2 = sw3 + kTcN * kTcOut, *sb3 = sb2 + kTcN;
+    float *ypart = sb3 + kTcOut;              // [2][kTcM][kTcOut]: the two column halves' outputs
+    float *sx = ypart + 2 * kTcM * kTcOut;    // the current tile's inputs, [kTcM][kTcIn]
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int ntiles = (rows + kTcM - 1) / kTcM;
+    const uint32_t sa_s = (uint32_t)__cvta_generic_to_shared(sa), sb_s = (uint32_t)__cvta_generic_to_shared(sb);
+    const uint32_t sx_s = (uint32_t)__cvta_generic_to_shared(sx);
+    auto load_x = [&](int tile) {  // one 16-byte chunk per thread
+        static_assert(kTcXBytes / 16 == kTcFwdThreads, "a tile's inputs are one chunk per thread");
+        const int m0 = tile * kTcM, r = t / 2;
+        const bool in = m0 + r < rows;
+        cp_async16(sx_s + 16 * t, x + (size_t)(in ? m0 + r : 0) * kTcIn + 4 * (t & 1), in ? 16u : 0u);
+    };
+    for (uint32_t i = t; i < kTcBBytes / 16; i += kTcFwdThreads) cp_async16(sb_s + 16 * i, wimg + 8 * i, 16u);
+    if ((int)blockIdx.x < ntiles) load_x(blockIdx.x);
+    for (int i = t; i < kTcN * kTcOut; i += kTcFwdThreads) sw3[i] = __bfloat162float(w3[i]);
+    for (int i = t; i < kTcN; i += kTcFwdThreads) sb2[i] = b2[i];
+    if (t < kTcOut) sb3[t] = b3[t];
+    // this lane's 8 columns of the first layer (the same for every row it computes)
+    const int k0 = lane * 8;
+    float w1r[kTcIn][8], b1r[8];
+#pragma unroll
+    for (int i = 0; i < kTcIn; ++i)
+#pragma unroll
+        for (int e = 0; e < 8; ++e) w1r[i][e] = __bfloat162float(w1[i * kTcN + k0 + e]);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) b1r[e] = b1[k0 + e];
+    // the first layer of a tile (its inputs in sx) into shared memory: warp w
+    // takes rows w, w + 8, ..., lane its 8 columns; rows past the end are zero
+    auto layer1 = [&](int tile) {
+        const int m0 = tile * kTcM;
+        for (int r = warp; r < kTcM; r += kTcFwdThreads / 32) {
+            __align__(16) __nv_bfloat16 hb[8];
+            if (m0 + r < rows) {
+                float xb[kTcIn];
+#pragma unroll
+                for (int i = 0; i < kTcIn; ++i) xb[i] = __bfloat162float(__float2bfloat16_rn(sx[r * kTcIn + i]));
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    float acc = 0.f;
+#pragma unroll
+                    for (int i = 0; i < kTcIn; ++i) acc = __fmaf_rn(xb[i], w1r[i][e], acc);
+                    hb[e] = __float2bfloat16_rn(fmaxf(__fadd_rn(acc, b1r[e]), 0.f));
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) hb[e] = __float2bfloat16_rn(0.f);
+            }
+            *reinterpret_cast<uint4 *>(sa + core_off(r, k0)) = *reinterpret_cast<const uint4 *>(hb);
+        }
+    };
+    const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(mbar);
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {  // two accumulators: 512 columns of tensor memory
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::
+                         "r"((uint32_t)__cvta_generic_to_shared(tmem_slot)), "r"(2u * kTcN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();  // the first tile's inputs and the tables are in place
+    if ((int)blockIdx.x < ntiles) layer1(blockIdx.x);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t idesc =
+        (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+    auto issue = [&](uint32_t acc_col) {  // one thread: the tile's product into the accumulator at acc_col
+#pragma unroll 1
+        for (int kk = 0; kk < kTcK / 16; ++kk) {
+            const uint64_t ad = smem_desc(sa_s + kk * 256, 128, (kTcK / 8) * 128);
+            const uint64_t bd = smem_desc(sb_s + kk * 256, 128, (kTcK / 8) * 128);
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem + acc_col),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(kk));
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_a)
+                     : "memory");
+    };
+    uint32_t phase = 0, buf = 0;
+    if (t == 0 && (int)blockIdx.x < ntiles) issue(0);
+    const int quarter = warp & 3, half = warp >> 2;  // accumulator lanes 32 * quarter.., columns 128 * half..
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int nxt = tile + gridDim.x;
+        if (nxt < ntiles) load_x(nxt);  // sx is free: this tile's first layer is done
+        // wait for this tile's product (bounded: a wait that gives up flags an error)
+        uint32_t done = 0;
+        for (uint32_t it = 0; it < kTcSpinLimit && !done; ++it)
+            asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                         " selp.u32 %0, 1, 0, p;\n}\n"
+                         : "=r"(done)
+                         : "r"(mbar_a), "r"(phase)
+                         : "memory");
+        phase ^= 1u;
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        done = __syncthreads_and(done);  // one decision for the CTA; the next inputs are in place
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (!done) {
+            atomicExch(&g_mlp_tc_error, 1u);
+            break;
+        }
+        // the next tile's first layer into the freed buffer, and its product
+        // into the other accumulator, while this tile's is read out
+        if (nxt < ntiles) {
+            layer1(nxt);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            if (t == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                issue((buf ^ 1u) * kTcN);
+            }
+        }
+        // epilogue: bias, ReLU, BF16 and the output layer over this warp's half of the columns
+        const int rl = quarter * 32 + lane;  // row within the tile
+        const uint32_t trow = tmem + buf * kTcN + ((uint32_t)(quarter * 32) << 16);
+        float yo[kTcOut] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+        for (int c = half * (kTcN / 2); c < (half + 1) * (kTcN / 2); c += 32) {
+            uint32_t v[32];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                : "r"(trow + (uint32_t)c));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int e = 0; e < 32; ++e) {
+                const float hv = __bfloat162float(
+                    __float2bfloat16_rn(fmaxf(__fadd_rn(__uint_as_float(v[e]), sb2[c + e]), 0.f)));
+#pragma unroll
+                for (int j = 0; j < kTcOut; ++j) yo[j] = __fmaf_rn(hv, sw3[(c + e) * kTcOut + j], yo[j]);
+            }
+        }
+        *reinterpret_cast<float4 *>(ypart + (half * kTcM + rl) * kTcOut) = make_float4(yo[0], yo[1], yo[2], yo[3]);
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();  // this accumulator is read before a later tile's product reuses it
+        if (half == 0) {
+            const int r = tile * kTcM + rl;
+            const float4 a0 = *reinterpret_cast<const float4 *>(ypart + rl * kTcOut);
+            const float4 a1 = *reinterpret_cast<const float4 *>(ypart + (kTcM + rl) * kTcOut);
+            if (r < rows)
+                *reinterpret_cast<float4 *>(y + (size_t)r * kTcOut) =
+                    make_float4(__fadd_rn(__fadd_rn(a0.x, a1.x), sb3[0]), __fadd_rn(__fadd_rn(a0.y, a1.y), sb3[1]),
+                                __fadd_rn(__fadd_rn(a0.z, a1.z), sb3[2]), __fadd_rn(__fadd_rn(a0.w, a1.w), sb3[3]));
+        }
+        buf ^= 1u;
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2u * kTcN));
+    }
+}
+
 // Mean squared error over rows x cols and its gradient 2 (y - t) / (rows * cols).
 __global__ void k_mlp_mse(const float *__restrict__ y, const float *__restrict__ t, int n, float scale,
                           float *__restrict__ dy, __nv_bfloat16 *__restrict__ dy16, double *loss)
@@ -563,7 +755,9 @@ int boids_mlp_create(int32_t n_in, int32_t n_hidden, int32_t n_out, uint64_t see
     if (ok && n_hidden == kTcN) {  // the hidden product on the tensor cores
         ok = cudaMalloc(&m->w2img, kTcBBytes) == cudaSuccess &&
              cudaFuncSetAttribute(k_mlp_hidden_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem) ==
-                 cudaSuccess;
+                 cudaSuccess &&
+             cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kTcFwdSmem) == cudaSuccess;
     }
     if (!ok) {
         cudaGetLastError();
@@ -617,8 +811,19 @@ int boids_mlp_forward(boids_mlp *m, const float *x, int32_t rows, float *y)
     if (rows == 0) return BOIDS_OK;
     cudaSetDevice(m->device);
     if (int rc = ensure_rows(m, rows)) return rc;
-    if (int rc = upload_rows(m, x, nullptr, rows)) return rc;
-    forward(m, rows, false);  // inference: the backward pass's pre-activations are not needed
+    if (m->w2img && m->in == kTcIn && m->out == kTcOut) {
+        // the fused pass: x in, y out, one kernel after the weight image
+        MCK(cudaMemcpyAsync(m->x, x, sizeof(float) * (size_t)rows * m->in, cudaMemcpyHostToDevice, m->st));
+        const __nv_bfloat16 *W1 = m->p16 + m->off[0], *W2 = m->p16 + m->off[2], *W3 = m->p16 + m->off[4];
+        const float *b1 = m->p + m->off[1], *b2 = m->p + m->off[3], *b3 = m->p + m->off[5];
+        k_mlp_tile_w<<<nb(kTcN * kTcK / 8, 256), 256, 0, m->st>>>(W2, m->w2img);
+        const unsigned tiles = nb(rows, kTcM);
+        k_mlp_forward_tc<<<tiles < m->nsm ? tiles : m->nsm, kTcFwdThreads, kTcFwdSmem, m->st>>>(
+            m->x, rows, W1, b1, m->w2img, b2, W3, b3, m->y);
+    } else {
+        if (int rc = upload_rows(m, x, nullptr, rows)) return rc;
+        forward(m, rows, false);  // inference: the backward pass's pre-activations are not needed
+    }
     MCK(cudaGetLastError());
     MCK(cudaMemcpyAsync(y, m->y, sizeof(float) * (size_t)rows * m->out, cudaMemcpyDeviceToHost, m->st));
     MCK(cudaStreamSynchronize(m->st));

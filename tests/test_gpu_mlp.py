@@ -40,7 +40,7 @@ def test_params_roundtrip(net):
     assert np.array_equal(net.params(), q)
 
 
-@pytest.mark.parametrize("rows", [1, 37, 1000])
+@pytest.mark.parametrize("rows", [1, 37, 1000, 40000])
 def test_forward_matches_oracle(net, rows):
     rng = np.random.default_rng(rows)
     p = net.params()
@@ -83,3 +83,20 @@ def test_training_fits_a_smooth_map(net):
     y1 = net.predict(x)
     loss1 = float(np.mean((y1 - t) ** 2))
     assert loss1 < 0.05 * loss0 and last < 0.05 * loss0
+
+
+def test_fused_inference_agrees_with_training_forward(net):
+    """Inference runs the whole network in one tensor-core kernel; the
+    training pass runs it layer by layer.  Both round at the same points, so
+    the loss of the fused outputs equals the training pass's loss up to FP32
+    summation order (the two sum in different orders)."""
+    rng = np.random.default_rng(5)
+    p = net.params()
+    p[N_IN * H:N_IN * H + H] = rng.normal(0, 0.1, H)
+    net.set_params(p)
+    x = rng.random((5000, N_IN), dtype=np.float32)
+    t = rng.random((5000, N_OUT), dtype=np.float32)
+    y = net.predict(x).astype(np.float64)
+    _, loss = net.gradient(x, t)
+    fused = float(np.mean((y - t) ** 2))
+    assert abs(fused - loss) <= 1e-4 * loss, (fused, loss)
