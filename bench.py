@@ -251,19 +251,17 @@ def ensemble_flocks(B, count, seed):
 
 def run_ensemble(a, B, rank, dist):
     """Sweep time of the whole ensemble for --ensemble-steps steps from its
-    initial state, with the per-flock statistics at the end.  The timed run
-    includes one retuning of the dense-cell thresholds once the flocks have
-    gathered (a quarter of the way in)."""
+    initial state, with the per-flock statistics at the end, on the default
+    dense-cell thresholds (a retune a quarter of the way in costs more in
+    trial steps than it wins)."""
     import numpy as np
     flocks, total = ensemble_flocks(B, a.ensemble_flocks, 2024 + 1000 * rank)
     ens = B.Ensemble(flocks)
     ens.init()
     ens.synchronize()
+    tuning = ens.tuning()
     t0 = time.perf_counter()
-    q = a.ensemble_steps // 4
-    ens.step(q)
-    tuning = ens.autotune(2)
-    ens.step(a.ensemble_steps - q)
+    ens.step(a.ensemble_steps)
     ens.synchronize()
     dt, units = reduce_over_ranks(dist, time.perf_counter() - t0, float(total * a.ensemble_steps))
     st = ens.stats()
@@ -275,8 +273,7 @@ def run_ensemble(a, B, rank, dist):
             "stats_mean": {k: float(np.mean(st[:, i])) for i, k in enumerate(B.STAT_NAMES[:4])},
             "config": "N log-uniform in [2^10, 2^16], F = (N/16384)^(1/3), marun2019 radii, weights "
                       "and vmax x U[0.7, 1.3], random_uniform init, steps replayed from CUDA graphs; "
-                      "timed from the initial state, including one autotune (2 steps per trial) "
-                      "after a quarter of the steps"}
+                      "timed from the initial state, default dense-cell thresholds"}
 
 
 # ------------------------------------------------------------------ our arm
