@@ -166,6 +166,11 @@ struct boids_sim {
     uint64_t graph_launches = 0;  // kernel launches per replay
     int graph_engine = -1;        // the kernels it was captured with
     bool graph_off = false;       // capture failed once on this handle
+    // set_state/get_state move the state in kXferChunks pieces of ids; with
+    // the side stream, one piece is packed (or copied out) while the next is
+    // copied (or unpacked): one event per piece
+    static constexpr int kXferChunks = 4;
+    cudaEvent_t xfer_ev[kXferChunks] = {};
 };
 
 namespace {
@@ -558,9 +563,36 @@ void boids_destroy(boids_sim *s)
         if (e) cudaEventDestroy(e);
     resolve_events(s);
     for (cudaEvent_t e : s->pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : s->xfer_ev)
+        if (e) cudaEventDestroy(e);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
 }
+
+namespace {
+
+// First id of transfer piece c (of kXferChunks), on a 1024-id boundary.
+uint32_t xfer_start(uint32_t n, int c)
+{
+    const uint64_t b = ((uint64_t)n * (uint32_t)c / boids_sim::kXferChunks + 1023) & ~(uint64_t)1023;
+    return (uint32_t)std::min<uint64_t>(b, n);
+}
+
+// Whether the transfers run in pieces: with the side stream, once the
+// pieces' events exist (made on first use; without them, one piece).
+bool xfer_pipelined(boids_sim *s)
+{
+    if (!s->b.aux) return false;
+    for (cudaEvent_t &ev : s->xfer_ev)
+        if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+            ev = nullptr;
+            cudaGetLastError();
+            return false;
+        }
+    return true;
+}
+
+}  // namespace
 
 int boids_set_state(boids_sim *s, const float *pos3n, const float *vel3n)
 {
@@ -573,16 +605,41 @@ int boids_set_state(boids_sim *s, const float *pos3n, const float *vel3n)
     // with its own kernels)
     const bool check = s->k.G != 0;
     float *dpos = s->b.stage, *dvel = s->b.stage + (size_t)3 * n;
+    const bool pipe = xfer_pipelined(s);
     {
         PhaseTimer t(s, 2);
-        if (check) CK(cudaMemsetAsync(s->b.flag, 0, sizeof(uint32_t), s->stream));
-        CK(cudaMemcpyAsync(dpos, pos3n, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s->stream));
-        CK(cudaMemcpyAsync(dvel, vel3n, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s->stream));
-        CK(boidsgpu::launch_pack(dpos, dvel, s->b.pos[0], s->b.vel[0], n, check ? s->b.flag : nullptr,
-                                 s->k.F_dn > s->k.Ff ? s->k.F_dn : s->k.Ff, s->stream, &s->launches));
+        if (check) {
+            CK(cudaMemsetAsync(s->b.flag, 0, sizeof(uint32_t), s->stream));
+            CK(cudaMemsetAsync(s->b.count, 0, sizeof(uint32_t) * s->b.ncell_pad, s->stream));
+        }
+        // each piece is copied in on the engine's stream and packed (and,
+        // for the grid, binned: the binning clamps every coordinate into the
+        // grid, so a state that fails the range check only wastes it) on
+        // the side stream while the next piece is copied
+        cudaStream_t ps = pipe ? s->b.aux : s->stream;
+        const int pieces = pipe ? boids_sim::kXferChunks : 1;
+        for (int c = 0; c < pieces; ++c) {
+            const uint32_t i0 = pipe ? xfer_start(n, c) : 0, i1 = pipe ? xfer_start(n, c + 1) : n;
+            if (i1 <= i0) continue;
+            const size_t off = (size_t)3 * i0, bytes = sizeof(float) * 3 * (size_t)(i1 - i0);
+            CK(cudaMemcpyAsync(dpos + off, pos3n + off, bytes, cudaMemcpyHostToDevice, s->stream));
+            CK(cudaMemcpyAsync(dvel + off, vel3n + off, bytes, cudaMemcpyHostToDevice, s->stream));
+            if (pipe) {
+                CK(cudaEventRecord(s->xfer_ev[c], s->stream));
+                CK(cudaStreamWaitEvent(ps, s->xfer_ev[c], 0));
+            }
+            CK(boidsgpu::launch_pack(dpos, dvel, s->b.pos[0], s->b.vel[0], i0, i1, check ? s->b.flag : nullptr,
+                                     s->k.F_dn > s->k.Ff ? s->k.F_dn : s->k.Ff, check ? &s->k : nullptr, s->b.key,
+                                     s->b.rank, s->b.count, ps, &s->launches));
+        }
+        if (pipe) {
+            CK(cudaEventRecord(s->b.join, ps));
+            CK(cudaStreamWaitEvent(s->stream, s->b.join, 0));
+        }
     }
     s->has_state = false;
     s->forces_valid = false;
+    s->cur = 0;
     if (check) {
         uint32_t bad = 0;
         CK(cudaMemcpyAsync(&bad, s->b.flag, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
@@ -591,8 +648,6 @@ int boids_set_state(boids_sim *s, const float *pos3n, const float *vel3n)
             return fail(BOIDS_EINVAL, "grid engine: positions must lie in [0, field_size]");
         s->engine = bad ? 0 : 1;
     }
-    s->cur = 0;
-    if (s->engine == 1 && (rc = grid_bin_fresh(s))) return rc;
     s->has_state = true;
     return BOIDS_OK;
 }
@@ -734,13 +789,35 @@ int boids_get_state(boids_sim *s, float *pos3n, float *vel3n)
     int rc = use_device(s);
     if (rc) return rc;
     const uint32_t n = s->k.n;
-    float *dpos = s->b.stage, *dvel = s->b.stage + (size_t)3 * n;
+    float *dpos = pos3n ? s->b.stage : nullptr, *dvel = vel3n ? s->b.stage + (size_t)3 * n : nullptr;
+    const bool pipe = xfer_pipelined(s);
     {
         PhaseTimer t(s, 2);
-        CK(boidsgpu::launch_unpack(s->b.pos[s->cur], s->b.vel[s->cur], pos3n ? dpos : nullptr,
-                                   vel3n ? dvel : nullptr, n, s->stream, &s->launches));
-        if (pos3n) CK(cudaMemcpyAsync(pos3n, dpos, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s->stream));
-        if (vel3n) CK(cudaMemcpyAsync(vel3n, dvel, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s->stream));
+        const float4 *p4 = s->b.pos[s->cur], *v4 = s->b.vel[s->cur];
+        // the other state buffer is dead between updates: it holds the
+        // id -> slot table
+        uint32_t *slot_of = reinterpret_cast<uint32_t *>(s->b.pos[1 - s->cur]);
+        CK(boidsgpu::launch_unpack_index(p4, slot_of, n, s->stream, &s->launches));
+        // each piece is unpacked on the engine's stream and copied out on
+        // the side stream while the next piece is unpacked
+        cudaStream_t cs = pipe ? s->b.aux : s->stream;
+        const int pieces = pipe ? boids_sim::kXferChunks : 1;
+        for (int c = 0; c < pieces; ++c) {
+            const uint32_t i0 = pipe ? xfer_start(n, c) : 0, i1 = pipe ? xfer_start(n, c + 1) : n;
+            if (i1 <= i0) continue;
+            const size_t off = (size_t)3 * i0, bytes = sizeof(float) * 3 * (size_t)(i1 - i0);
+            CK(boidsgpu::launch_unpack_gather(p4, v4, slot_of, dpos, dvel, i0, i1, n, s->stream, &s->launches));
+            if (pipe) {
+                CK(cudaEventRecord(s->xfer_ev[c], s->stream));
+                CK(cudaStreamWaitEvent(cs, s->xfer_ev[c], 0));
+            }
+            if (pos3n) CK(cudaMemcpyAsync(pos3n + off, dpos + off, bytes, cudaMemcpyDeviceToHost, cs));
+            if (vel3n) CK(cudaMemcpyAsync(vel3n + off, dvel + off, bytes, cudaMemcpyDeviceToHost, cs));
+        }
+        if (pipe) {
+            CK(cudaEventRecord(s->b.join, cs));
+            CK(cudaStreamWaitEvent(s->stream, s->b.join, 0));
+        }
     }
     return boids_synchronize(s);
 }

@@ -174,9 +174,20 @@ constexpr int kMaxGridAxis = 812;          // device cells per axis: 4 G^3 < 2^3
 
 // Launchers.  Each returns the launch's cudaError_t and adds the number of
 // kernels it launched to *launches.
-cudaError_t launch_pack(const float *pos3, const float *vel3, float4 *pos4, float4 *vel4,
-                        uint32_t n, uint32_t *bad, float hi, cudaStream_t s, uint64_t *launches);
-cudaError_t launch_unpack(const float4 *pos4, const float4 *vel4, float *pos3, float *vel3,
+// Packs ids [i0, i1) of an id-ordered state (slot = id); bad: the range
+// check's flag (nullable); bin (nullable): also the grid keys of those slots,
+// as launch_grid_keys (a single flock; count cleared beforehand).
+cudaError_t launch_pack(const float *pos3, const float *vel3, float4 *pos4, float4 *vel4, uint32_t i0, uint32_t i1,
+                        uint32_t *bad, float hi, const StepConst *bin, uint32_t *key, uint32_t *rank,
+                        uint32_t *count, cudaStream_t s, uint64_t *launches);
+// Slot order -> id order: the slot of every id into slot_of (n words of
+// scratch), then ids [i0, i1) gathered into pos3/vel3 (either nullable).
+cudaError_t launch_unpack_index(const float4 *pos4, uint32_t *slot_of, uint32_t n, cudaStream_t s,
+                                uint64_t *launches);
+cudaError_t launch_unpack_gather(const float4 *pos4, const float4 *vel4, const uint32_t *slot_of, float *pos3,
+                                 float *vel3, uint32_t i0, uint32_t i1, uint32_t n, cudaStream_t s,
+                                 uint64_t *launches);
+cudaError_t launch_unpack(const float4 *pos4, const float4 *vel4, uint32_t *slot_of, float *pos3, float *vel3,
                           uint32_t n, cudaStream_t s, uint64_t *launches);
 // One .ptcl frame in id order: pframe gets 3 floats per boid, or 12 with
 // forces (xyz + the nine get_force floats; zeros when force9 is null);

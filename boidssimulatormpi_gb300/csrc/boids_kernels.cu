@@ -347,32 +347,57 @@ __device__ __forceinline__ void finish_boid(const Acc &a, float4 p4, float3 vi, 
 
 // ------------------------------------------------------------------ state packing
 
-// Packs an id-ordered state into float4 records (w of pos = id bits).  With
-// bad != null, a coordinate outside [0, hi] (or NaN) sets *bad.
+// Packs ids [i0, i1) of an id-ordered state into float4 records, slot = id
+// (w of pos = id bits).  With bad != null, a coordinate outside [0, hi] (or
+// NaN) sets *bad.  With key != null the boid is also binned for the grid
+// (k_grid_keys' work, fused): cell_key clamps every coordinate into the
+// grid, so a state that fails the range check still bins in bounds.
 __global__ void k_pack(const float *__restrict__ pos3, const float *__restrict__ vel3,
-                       float4 *__restrict__ pos4, float4 *__restrict__ vel4, uint32_t n,
-                       uint32_t *__restrict__ bad, float hi)
+                       float4 *__restrict__ pos4, float4 *__restrict__ vel4, uint32_t i0, uint32_t i1,
+                       uint32_t *__restrict__ bad, float hi, uint32_t *__restrict__ key,
+                       uint32_t *__restrict__ rank, uint32_t *__restrict__ count, StepConst k)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float x = pos3[3 * i], y = pos3[3 * i + 1], z = pos3[3 * i + 2];
+    const uint32_t i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= i1) return;
+    const float x = pos3[3 * (size_t)i], y = pos3[3 * (size_t)i + 1], z = pos3[3 * (size_t)i + 2];
     pos4[i] = make_float4(x, y, z, __uint_as_float(i));
-    vel4[i] = make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.f);
+    vel4[i] = make_float4(vel3[3 * (size_t)i], vel3[3 * (size_t)i + 1], vel3[3 * (size_t)i + 2], 0.f);
     if (bad && !(x >= 0.f && x <= hi && y >= 0.f && y <= hi && z >= 0.f && z <= hi)) *bad = 1u;
+    if (key) {
+        const uint32_t c = k.cell_base + cell_key(make_float3(x, y, z), k);
+        key[i] = c;
+        rank[i] = atomicAdd(count + c, 1u);
+    }
 }
 
-// Slot order -> id order (the reference's getters index by id).
-__global__ void k_unpack(const float4 *__restrict__ pos4, const float4 *__restrict__ vel4,
-                         float *__restrict__ pos3, float *__restrict__ vel3, uint32_t n)
+// Slot order -> id order (the reference's getters index by id), first pass:
+// the slot of every id.  A valid state holds each id in [0, n) once; other
+// ids are skipped.
+__global__ void k_unpack_index(const float4 *__restrict__ pos4, uint32_t *__restrict__ slot_of, uint32_t n)
 {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    const float4 p = pos4[s];
-    const uint32_t id = __float_as_uint(p.w);
-    if (pos3) { pos3[3 * id] = p.x; pos3[3 * id + 1] = p.y; pos3[3 * id + 2] = p.z; }
+    const uint32_t id = __float_as_uint(__ldg(reinterpret_cast<const float *>(pos4) + 4 * (size_t)s + 3));
+    if (id < n) slot_of[id] = s;
+}
+
+// Second pass, ids [i0, i1): a thread per id gathers its records, so that a
+// warp's stores are contiguous (a thread per slot would scatter six 4-byte
+// stores to random ids).
+__global__ void k_unpack_gather(const float4 *__restrict__ pos4, const float4 *__restrict__ vel4,
+                                const uint32_t *__restrict__ slot_of, float *__restrict__ pos3,
+                                float *__restrict__ vel3, uint32_t i0, uint32_t i1, uint32_t n)
+{
+    const uint32_t i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= i1) return;
+    const uint32_t s = min(__ldg(slot_of + i), n - 1);
+    if (pos3) {
+        const float4 p = __ldg(pos4 + s);
+        pos3[3 * (size_t)i] = p.x; pos3[3 * (size_t)i + 1] = p.y; pos3[3 * (size_t)i + 2] = p.z;
+    }
     if (vel3) {
-        const float4 v = vel4[s];
-        vel3[3 * id] = v.x; vel3[3 * id + 1] = v.y; vel3[3 * id + 2] = v.z;
+        const float4 v = __ldg(vel4 + s);
+        vel3[3 * (size_t)i] = v.x; vel3[3 * (size_t)i + 1] = v.y; vel3[3 * (size_t)i + 2] = v.z;
     }
 }
 
@@ -1874,22 +1899,43 @@ __global__ void k_ref_cells(const float4 *__restrict__ pos, int32_t *__restrict_
 
 static inline unsigned blocks_for(uint32_t n, unsigned t) { return (n + t - 1) / t; }
 
-cudaError_t launch_pack(const float *pos3, const float *vel3, float4 *pos4, float4 *vel4, uint32_t n,
-                        uint32_t *bad, float hi, cudaStream_t st, uint64_t *launches)
+cudaError_t launch_pack(const float *pos3, const float *vel3, float4 *pos4, float4 *vel4, uint32_t i0, uint32_t i1,
+                        uint32_t *bad, float hi, const StepConst *bin, uint32_t *key, uint32_t *rank,
+                        uint32_t *count, cudaStream_t st, uint64_t *launches)
 {
-    if (n == 0) return cudaSuccess;
-    k_pack<<<blocks_for(n, 256), 256, 0, st>>>(pos3, vel3, pos4, vel4, n, bad, hi);
+    if (i1 <= i0) return cudaSuccess;
+    const StepConst none{};
+    k_pack<<<blocks_for(i1 - i0, 256), 256, 0, st>>>(pos3, vel3, pos4, vel4, i0, i1, bad, hi, bin ? key : nullptr,
+                                                      rank, count, bin ? *bin : none);
     ++*launches;
     return cudaGetLastError();
 }
 
-cudaError_t launch_unpack(const float4 *pos4, const float4 *vel4, float *pos3, float *vel3, uint32_t n,
-                          cudaStream_t st, uint64_t *launches)
+cudaError_t launch_unpack_index(const float4 *pos4, uint32_t *slot_of, uint32_t n, cudaStream_t st,
+                                uint64_t *launches)
 {
     if (n == 0) return cudaSuccess;
-    k_unpack<<<blocks_for(n, 256), 256, 0, st>>>(pos4, vel4, pos3, vel3, n);
+    k_unpack_index<<<blocks_for(n, 256), 256, 0, st>>>(pos4, slot_of, n);
     ++*launches;
     return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_gather(const float4 *pos4, const float4 *vel4, const uint32_t *slot_of, float *pos3,
+                                 float *vel3, uint32_t i0, uint32_t i1, uint32_t n, cudaStream_t st,
+                                 uint64_t *launches)
+{
+    if (i1 <= i0) return cudaSuccess;
+    k_unpack_gather<<<blocks_for(i1 - i0, 256), 256, 0, st>>>(pos4, vel4, slot_of, pos3, vel3, i0, i1, n);
+    ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack(const float4 *pos4, const float4 *vel4, uint32_t *slot_of, float *pos3, float *vel3,
+                          uint32_t n, cudaStream_t st, uint64_t *launches)
+{
+    cudaError_t e = launch_unpack_index(pos4, slot_of, n, st, launches);
+    if (e != cudaSuccess) return e;
+    return launch_unpack_gather(pos4, vel4, slot_of, pos3, vel3, 0, n, n, st, launches);
 }
 
 cudaError_t launch_frame(const float4 *pos4, const float4 *vel4, const float *force9, float *pframe,

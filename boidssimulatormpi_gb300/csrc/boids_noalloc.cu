@@ -206,14 +206,15 @@ extern "C" int boids_step_noalloc(const boids_params *params, const float *pos3n
     // the array keeps the previous call's contents: clear what must start at zero
     if ((e = cudaMemsetAsync(b.count, 0, 4 * (size_t)b.ncell_pad, st)) == cudaSuccess &&
         (e = cudaMemsetAsync(b.ticket, 0, 4, st)) == cudaSuccess &&
-        (e = boidsgpu::launch_pack(pos3n_in, vel3n_in, b.pos[0], b.vel[0], n, nullptr, 0.f, st, &launches)) ==
-            cudaSuccess &&
-        (e = boidsgpu::launch_grid_keys(k, b.pos[0], b.key, b.rank, b.count, st, &launches)) == cudaSuccess &&
+        (e = boidsgpu::launch_pack(pos3n_in, vel3n_in, b.pos[0], b.vel[0], 0, n, nullptr, 0.f, &k, b.key, b.rank,
+                                   b.count, st, &launches)) == cudaSuccess &&
         (e = boidsgpu::launch_grid_scan(k, b, st, &launches)) == cudaSuccess &&
         (e = boidsgpu::launch_grid_scatter(k, b, 0, true, st, &launches)) == cudaSuccess &&
         (e = boidsgpu::launch_grid_force(k, b, 1, false, false, st, &launches)) == cudaSuccess &&
-        (e = boidsgpu::launch_unpack(b.pos[0], b.vel[0], pos3n_out, vel3n_out, n, st, &launches)) ==
-            cudaSuccess) {
+        // the sorted copy in b.pos[1] is dead once the rules have run: it
+        // holds the id -> slot table of the unpacking
+        (e = boidsgpu::launch_unpack(b.pos[0], b.vel[0], reinterpret_cast<uint32_t *>(b.pos[1]), pos3n_out,
+                                     vel3n_out, n, st, &launches)) == cudaSuccess) {
         return BOIDS_OK;
     }
     char msg[160];
