@@ -157,15 +157,20 @@ struct boids_sim {
     // completion event per slot, made on first use
     float *frame_dev = nullptr;
     cudaEvent_t frame_ev[BOIDS_FRAME_SLOTS] = {};
-    // kGraphSteps updates captured into a CUDA graph on first use; valid for
-    // the stream, buffer parity and constants it was captured with
-    cudaGraphExec_t graph = nullptr;
-    cudaStream_t graph_stream = nullptr;
-    int graph_cur = -1;
-    StepConst graph_k{};
-    uint64_t graph_launches = 0;  // kernel launches per replay
-    int graph_engine = -1;        // the kernels it was captured with
-    bool graph_off = false;       // capture failed once on this handle
+    // Updates captured into CUDA graphs on first use: [0] kGraphSteps
+    // updates, for long runs; [1] one update of the grid engine, so that a
+    // single update's kernels reach the GPU in one launch.  Each is valid for
+    // the stream, buffer parity and constants it was captured with.
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        cudaStream_t stream = nullptr;
+        int cur = -1;
+        StepConst k{};
+        uint64_t launches = 0;  // kernel launches per replay
+        int engine = -1;        // the kernels it was captured with
+    };
+    StepGraph graphs[2];
+    bool graph_off = false;     // capture failed once on this handle
     // set_state/get_state move the state in kXferChunks pieces of ids; with
     // the side stream, one piece is packed (or copied out) while the next is
     // copied (or unpacked): one event per piece
@@ -557,7 +562,8 @@ void boids_destroy(boids_sim *s)
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->b.aux) cudaStreamSynchronize(s->b.aux);
     free_buffers(s->b);
-    if (s->graph) cudaGraphExecDestroy(s->graph);
+    for (auto &gr : s->graphs)
+        if (gr.exec) cudaGraphExecDestroy(gr.exec);
     if (s->frame_dev) cudaFree(s->frame_dev);
     for (cudaEvent_t e : s->frame_ev)
         if (e) cudaEventDestroy(e);
@@ -711,17 +717,19 @@ int step_once(boids_sim *s, bool rec)
     return 0;
 }
 
-// The graph of kGraphSteps updates for the handle's current stream, buffer
-// parity and constants, captured if needed; false when it cannot be had.
-bool graph_ready(boids_sim *s, bool rec)
+// Graph `which` (0: kGraphSteps updates, 1: one update) for the handle's
+// current stream, buffer parity and constants, captured if needed; false
+// when it cannot be had.
+bool graph_ready(boids_sim *s, bool rec, int which)
 {
     if (s->graph_off || !s->stream) return false;  // the legacy stream cannot be captured
-    if (s->graph && s->graph_stream == s->stream && s->graph_cur == s->cur && s->graph_engine == s->engine &&
-        std::memcmp(&s->graph_k, &s->k, sizeof(StepConst)) == 0)
+    boids_sim::StepGraph &gr = s->graphs[which];
+    if (gr.exec && gr.stream == s->stream && gr.cur == s->cur && gr.engine == s->engine &&
+        std::memcmp(&gr.k, &s->k, sizeof(StepConst)) == 0)
         return true;
-    if (s->graph) {
-        cudaGraphExecDestroy(s->graph);
-        s->graph = nullptr;
+    if (gr.exec) {
+        cudaGraphExecDestroy(gr.exec);
+        gr.exec = nullptr;
     }
     if (boidsgpu::grid_prepare() != cudaSuccess) {  // function attributes are set outside the capture
         cudaGetLastError();
@@ -731,17 +739,18 @@ bool graph_ready(boids_sim *s, bool rec)
     const uint64_t launches = s->launches, done = s->steps_done;
     const boids_profile_t acc = s->acc;
     const int cur = s->cur;
+    const int steps = which == 0 ? kGraphSteps : 1;
     cudaGraph_t g = nullptr;
     bool ok = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-    for (int t = 0; ok && t < kGraphSteps; ++t) ok = step_once(s, rec) == 0;
+    for (int t = 0; ok && t < steps; ++t) ok = step_once(s, rec) == 0;
     if (cudaStreamEndCapture(s->stream, &g) != cudaSuccess) ok = false;
-    s->graph_launches = s->launches - launches;
+    gr.launches = s->launches - launches;
     s->launches = launches;
     s->steps_done = done;
     s->acc = acc;
     s->cur = cur;  // nothing ran: only recorded
-    if (ok && cudaGraphInstantiate(&s->graph, g, 0) != cudaSuccess) {
-        s->graph = nullptr;
+    if (ok && cudaGraphInstantiate(&gr.exec, g, 0) != cudaSuccess) {
+        gr.exec = nullptr;
         ok = false;
     }
     if (g) cudaGraphDestroy(g);
@@ -750,10 +759,10 @@ bool graph_ready(boids_sim *s, bool rec)
         s->graph_off = true;
         return false;
     }
-    s->graph_stream = s->stream;
-    s->graph_cur = s->cur;
-    s->graph_k = s->k;
-    s->graph_engine = s->engine;
+    gr.stream = s->stream;
+    gr.cur = s->cur;
+    gr.k = s->k;
+    gr.engine = s->engine;
     return true;
 }
 
@@ -767,13 +776,26 @@ int boids_step(boids_sim *s, int32_t steps)
     if (rc) return rc;
     const bool rec = s->b.forces != nullptr;
     int32_t t = 0;
-    // long runs replay captured graphs (not while timing phases with events)
-    if (steps >= 2 * kGraphSteps && !s->prof && graph_ready(s, rec)) {
-        for (; steps - t >= kGraphSteps; t += kGraphSteps) {
-            CK(cudaGraphLaunch(s->graph, s->stream));
-            s->launches += s->graph_launches;
-            s->steps_done += kGraphSteps;
-            s->acc.steps += kGraphSteps;
+    // replays of captured graphs (not while timing phases with events): the
+    // long runs' kGraphSteps updates at a time, the grid engine's other
+    // updates one at a time (the all-pairs engine swaps its state buffers
+    // every update, so its single updates are launched directly)
+    if (!s->prof) {
+        if (steps >= 2 * kGraphSteps && graph_ready(s, rec, 0)) {
+            for (; steps - t >= kGraphSteps; t += kGraphSteps) {
+                CK(cudaGraphLaunch(s->graphs[0].exec, s->stream));
+                s->launches += s->graphs[0].launches;
+                s->steps_done += kGraphSteps;
+                s->acc.steps += kGraphSteps;
+            }
+        }
+        if (t < steps && s->engine == 1 && graph_ready(s, rec, 1)) {
+            for (; t < steps; ++t) {
+                CK(cudaGraphLaunch(s->graphs[1].exec, s->stream));
+                s->launches += s->graphs[1].launches;
+                s->steps_done += 1;
+                s->acc.steps += 1;
+            }
         }
     }
     for (; t < steps; ++t)

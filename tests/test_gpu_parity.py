@@ -349,6 +349,45 @@ def test_allpairs_engine_kernel_choice(boids_lib, oracle_mod):
         assert_bits_equal(sim.forces(), of, "forces (outside=%s)" % outside)
 
 
+def test_grid_engine_refuses_states_outside_the_field(boids_lib, oracle_mod):
+    """The grid engine bins positions in [0, F]: boids_set_state refuses a
+    state with a coordinate outside it, or NaN, wherever that boid sits among
+    the pieces the state is copied in, and the handle is then without a
+    state.  Coordinates 0 and F are inside.  A good state set afterwards
+    runs bit-exact."""
+    O = oracle_mod
+    n, field = 5000, 1.0
+    p = make_params(O, n, field, O.MARUN2019)
+    rng = np.random.default_rng(7)
+    pos = rng.random((n, 3), dtype=np.float32)
+    vel = (0.004 * rng.standard_normal((n, 3))).astype(np.float32)
+    sim = make_sim(boids_lib, "grid", n, field, O.MARUN2019)
+    sim.set_state(pos, vel)
+    sim.update(1)
+    above = np.nextafter(np.float32(field), np.float32(2))
+    for i, c, v in ((0, 0, np.float32(-1e-7)), (2047, 1, above), (3100, 0, np.float32(np.inf)),
+                    (4999, 2, np.float32(np.nan))):
+        q = pos.copy()
+        q[i, c] = v
+        with pytest.raises(boids_lib.BoidsError, match="positions must lie"):
+            sim.set_state(q, vel)
+        with pytest.raises(boids_lib.BoidsError, match="no state"):
+            sim.update(1)
+    q = pos.copy()
+    q[10] = field
+    q[4998] = 0.0
+    sim.set_state(q, vel)
+    assert_bits_equal(sim.state()[0], q, "positions on the faces")
+    sim.set_state(pos, vel)
+    sim.update(3)
+    op, ov, of = _oracle_run(O, p, "grid", pos.reshape(-1), vel.reshape(-1), 3)
+    gp, gv = sim.state()
+    assert_bits_equal(gp, op, "positions")
+    assert_bits_equal(gv, ov, "velocities")
+    assert_bits_equal(sim.forces(), of, "forces")
+    sim.close()
+
+
 def test_all_round_angles_and_test_ini(boids_lib, oracle_mod):
     """Sight angles >= 1 skip the cone test entirely (src/boid.cpp:29-31)."""
     O = oracle_mod
@@ -550,8 +589,10 @@ def test_handle_autotune_keeps_the_trajectory(boids_lib, oracle_mod):
 
 @pytest.mark.parametrize("engine", ["grid", "allpairs", "pairs"])
 def test_graph_replayed_steps_equal_single_steps(boids_lib, oracle_mod, engine):
-    """boids_step(sim, k >= 32) replays captured 16-update graphs; the same
-    updates one call at a time give the same bits and the same launch count."""
+    """boids_step(sim, k >= 32) replays captured 16-update graphs, and the
+    grid engine's other updates replay a one-update graph; the same updates
+    launched directly, one call at a time (phase timing on, which launches
+    every kernel itself), give the same bits and the same launch count."""
     O = oracle_mod
     prm = O.MARUN2019
     n, field = (12000, 0.91) if engine == "grid" else (3000, 0.6)
@@ -559,8 +600,9 @@ def test_graph_replayed_steps_equal_single_steps(boids_lib, oracle_mod, engine):
     b = make_sim(boids_lib, engine, n, field, prm)
     for s in (a, b):
         s.init()
+    b.profile_enable(True)
     la, lb = a.kernel_launches(), b.kernel_launches()
-    a.update(70)          # 4 graph replays + 6 direct updates
+    a.update(70)          # 4 replays of 16 updates + 6 single updates
     for _ in range(70):
         b.update(1)
     pa, va = a.state()
@@ -575,6 +617,11 @@ def test_graph_replayed_steps_equal_single_steps(boids_lib, oracle_mod, engine):
     for _ in range(40):
         b.update(1)
     assert_bits_equal(a.state()[0], b.state()[0], "positions after retuning")
+    for _ in range(5):   # single updates
+        a.update(1)
+    b.update(5)
+    assert_bits_equal(a.state()[0], b.state()[0], "positions after single updates")
+    assert_bits_equal(a.forces(), b.forces(), "forces after single updates")
 
 
 @pytest.mark.parametrize("engine", ["grid", "allpairs"])
