@@ -13,9 +13,10 @@
  * reference's getters and its .ptcl frames use.  Every call returns
  * BOIDS_OK (0) or a negative status; boids_last_error() gives the message.
  * Nothing calls exit().  A handle is not thread-safe; all of its GPU work is
- * ordered on one CUDA stream (a grid update forks part of its work onto a
- * side stream of the handle and joins it back before the update ends, so
- * work queued after it on the stream sees the finished state).
+ * ordered on one CUDA stream (a grid update, boids_set_state and
+ * boids_get_state fork part of their work onto a side stream of the handle
+ * and join it back before they end, so work queued after them on the stream
+ * sees their results).
  */
 #ifndef BOIDS_GB300_H
 #define BOIDS_GB300_H
@@ -132,7 +133,9 @@ int boids_set_state(boids_sim *sim, const float *pos3n, const float *vel3n);
 /* BoidSimulation::update (src/boid_simulation_grid.cpp:165-293), `steps`
  * times.  Asynchronous on the handle's stream.  A call of 32 or more steps
  * captures 16 updates into a CUDA graph once (per stream, buffer parity and
- * tuning) and replays it; results are the same bits either way. */
+ * tuning) and replays it; the grid engine's other updates replay a captured
+ * one-update graph; with profiling on every kernel is launched directly.
+ * Results are the same bits either way. */
 int boids_step(boids_sim *sim, int32_t steps);
 
 /* BoidSimulation::get(id, &x,&y,&z, &vx,&vy,&vz) for every id
