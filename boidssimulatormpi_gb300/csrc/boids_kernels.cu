@@ -694,8 +694,11 @@ __device__ __forceinline__ uint32_t sparse_segments(SparseSmem &sm, int t, float
         const float rem = k.trim_r2 - ddy * ddy - ddz * ddz;
         if (!(rem > 0.f)) continue;
         const float rx = sqrtf(rem);
-        const int lo = __float2int_rd((pi.x - rx) * k.inv_subx);
-        const int hi = __float2int_rd((pi.x + rx) * k.inv_subx);
+        // a boid in the field reaches at most one row length beyond either
+        // end; the clamp only keeps a state outside the field (never made
+        // by the update, refused by boids_set_state) within the cell tables
+        const int lo = max(__float2int_rd((pi.x - rx) * k.inv_subx), 1 - Gx);
+        const int hi = min(__float2int_rd((pi.x + rx) * k.inv_subx), 2 * Gx - 2);
         int a0 = lo, a1 = hi + 1, c0 = 0, c1 = 0;  // x-cell runs [a0, a1) and [c0, c1)
         uint32_t ca = 0, cb = 0;  // x shifts of the runs, 2-bit two's complement: 3 = -F, 1 = +F
         if (lo < 0) { a0 = lo + Gx; a1 = Gx; ca = 3; c1 = min(hi + 1, Gx); }

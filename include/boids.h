@@ -318,7 +318,9 @@ int boids_mlp_train(boids_mlp *mlp, const float *x, const float *target, int32_t
  * cudaMalloc/cudaFree, which can synchronize the device.  Inputs and outputs
  * are caller-owned DEVICE arrays in id order (3 floats per boid, xyz); in and
  * out must not overlap.  params->engine must be BOIDS_ENGINE_GRID; positions
- * must lie in [0, field_size] (not checked here).
+ * must lie in [0, field_size].  This call does not check them: other
+ * positions give meaningless results, but the kernels clamp every index they
+ * derive from a position, so they stay within their buffers.
  *
  * All scratch lives in one static device array of BOIDS_NOALLOC_SCRATCH_BYTES
  * that every GPU loading the library holds until the process exits; a step
