@@ -166,8 +166,8 @@ inline size_t dense_list_capacity(size_t ncell, size_t n)
     const size_t by_cells = ncell / 4;
     return 2 * ((by_cells < n ? by_cells : n) + n / kDenseRound + 1);
 }
-constexpr int kDenseCap = 768;        // candidates of a dense cell held in shared memory
-constexpr int kDenseCtasPerSm = 6;   // resident CTAs of the dense-cell kernel per SM (its launch bounds)
+constexpr int kDenseCap = 512;        // candidates of a dense cell held in shared memory
+constexpr int kDenseCtasPerSm = 7;   // resident CTAs of the dense-cell kernel per SM (its launch bounds)
 constexpr int kApCap = 256;           // all-pairs engine: neighbours kept per boid (more: an O(N) scan)
 constexpr uint32_t kMaxBoids = 1u << 29;  // slot index packs into 29 bits
 constexpr int kMaxGridAxis = 812;          // device cells per axis: 4 G^3 < 2^31

@@ -1301,7 +1301,7 @@ __device__ __forceinline__ void dense_hash_job(const DenseSmem &sm, const uint32
 // running count passes kDenseCap; if the first bin alone is over, the span
 // narrows to that bin.  A boid is a candidate at most once (G >= 3), so a
 // bin one id wide always fits and the search ends.
-constexpr int kWinBins = 1536;
+constexpr int kWinBins = 1024;
 
 __device__ uint32_t dense_window(DenseSmem &sm, const GridIn &g, int ns, uint32_t lo, uint32_t nid)
 {
