@@ -469,6 +469,12 @@ def run_ours(a):
     # ---- end to end through the C ABI with host buffers
     hp = torch.empty(3 * a.n, dtype=torch.float32, pin_memory=True).numpy()
     hv = torch.empty(3 * a.n, dtype=torch.float32, pin_memory=True).numpy()
+    for i in range(max(1, min(a.warmup, 3))):  # untimed: pinned pages touched, graphs captured
+        hp[:] = pos0.reshape(-1)
+        hv[:] = vel0.reshape(-1)
+        sim.set_state(hp, hv)
+        sim.update(1)
+        sim.state(hp, hv)
     hp[:] = pos0.reshape(-1)
     hv[:] = vel0.reshape(-1)
     barrier()

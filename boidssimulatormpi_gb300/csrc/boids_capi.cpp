@@ -598,6 +598,8 @@ bool xfer_pipelined(boids_sim *s)
     return true;
 }
 
+bool graph_ready(boids_sim *s, bool rec, int which);
+
 }  // namespace
 
 int boids_set_state(boids_sim *s, const float *pos3n, const float *vel3n)
@@ -655,6 +657,10 @@ int boids_set_state(boids_sim *s, const float *pos3n, const float *vel3n)
         s->engine = bad ? 0 : 1;
     }
     s->has_state = true;
+    // the grid engine's one-update graph, captured now if the constants,
+    // stream or kernels changed, so that the next update is not the one to
+    // wait for the capture (a failed capture only turns the graphs off)
+    if (s->engine == 1 && !s->prof) graph_ready(s, s->b.forces != nullptr, 1);
     return BOIDS_OK;
 }
 
