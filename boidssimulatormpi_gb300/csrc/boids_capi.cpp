@@ -184,7 +184,7 @@ void free_buffers(DevBuffers &b)
 {
     void *ptrs[] = {b.pos[0], b.pos[1], b.vel[0], b.vel[1], b.key, b.rank, b.count, b.lstart,
                     b.bsum, b.ticket, b.ap_cnt, b.ap_list, b.forces, b.stage, b.cells8, b.dcnt, b.dhash,
-                    b.dense_list, b.dense_n, b.flag, b.dflag, b.carry, b.defer, b.wscratch};
+                    b.dense_list, b.dense_n, b.flag, b.dflag, b.carry, b.defer, b.ovf, b.ovf_n, b.wscratch};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (b.aux) cudaStreamDestroy(b.aux);
@@ -521,6 +521,8 @@ int boids_create(const boids_params *params, boids_sim **out)
         }
         ALLOC(&b.dense_n, 3, true);
         ALLOC(&b.defer, 2 * n);
+        ALLOC(&b.ovf, (size_t)boidsgpu::kOvfCap * n);
+        ALLOC(&b.ovf_n, n);
         b.defer_cnt = b.dense_n + 2;
         if (cudaStreamCreateWithFlags(&b.aux, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming) != cudaSuccess ||

@@ -115,6 +115,9 @@ struct DevBuffers {
     uint32_t *defer;           // sparse boids deferred to further passes: (slot, lo_id), 2 words per slot (null: none);
                                // a flock's entries start at its slot_base
     uint32_t *defer_cnt;       // deferred boids per flock (a single flock: dense_n + 2)
+    uint64_t *ovf;             // per slot, kOvfCap entries: the accepted neighbours a deferred boid's
+                               // first pass could not keep (null: none)
+    uint32_t *ovf_n;           // per slot: how many there were (over kOvfCap: the row is incomplete)
     uint64_t *wscratch;        // dense kernel: wcap entries per CTA, a huge cell's candidates filed by window
     uint32_t wcap;             // (null / 0: every window scans the neighbourhood)
     // Side stream on which the deferred boids run beside the dense kernel,
@@ -131,6 +134,7 @@ struct DevBuffers {
 
 constexpr int kScanTile = 2048;       // cells per scan block (256 threads x 8)
 constexpr int kListCap = 12;          // grid engine, thread-per-boid kernel: sorted neighbours kept per pass
+constexpr int kOvfCap = 24;           // accepted neighbours beyond those a deferred boid's first pass keeps
 // Defaults, measured on the bench workload (N = 2^20 from a uniform start,
 // steps 5-25), the same flock after 1000 steps, and gathered flocks of 16 384
 // and 65 536 boids: dense_min 16 beats 12 on all four (3-6 %); lone_cand 64

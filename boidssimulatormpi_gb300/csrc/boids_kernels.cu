@@ -310,6 +310,8 @@ struct GridOut {
     Acc *carry;  // per slot: partial sums of huge cells between id windows (null: no windows)
     uint32_t *defer, *defer_cnt;  // k_grid_sparse's deferred boids: (slot, lo_id) pairs from the flock's slot_base,
                                   // and their count per flock (null: none)
+    uint64_t *ovf;                // per slot, kOvfCap: a deferred boid's accepted neighbours beyond its list
+    uint32_t *ovf_n;              // per slot: their number (null: not recorded)
     uint64_t *wscratch;           // k_grid_dense: wcap entries per CTA for bucketing huge cells' windows (null: none)
     uint32_t wcap;
 };
@@ -732,16 +734,45 @@ __device__ __forceinline__ uint32_t sparse_segments(SparseSmem &sm, int t, float
     return ncand;
 }
 
+// The m neighbours of the thread's column of sm.lst (sorted by id) added to
+// a in that order, each entry's loads issued one entry ahead.
+template <bool DIAG>
+__device__ __forceinline__ void list_accumulate(const SparseSmem &sm, int t, int m, float3 pi, Acc &a,
+                                                const GridIn &g, const StepConst &k)
+{
+    uint64_t e_next = m > 0 ? sm.lst[0][t] : 0;
+    float4 p_next = make_float4(0.f, 0.f, 0.f, 0.f), v_next = p_next;
+    if (m > 0) {
+        p_next = __ldg(g.pos + ((uint32_t)e_next & 0x1fffffffu));
+        v_next = __ldg(g.vel + ((uint32_t)e_next & 0x1fffffffu));
+    }
+    for (int q = 0; q < m; ++q) {
+        const uint64_t e = e_next;
+        const float4 pj = p_next, vv = v_next;
+        if (q + 1 < m) {
+            e_next = sm.lst[q + 1][t];
+            p_next = __ldg(g.pos + ((uint32_t)e_next & 0x1fffffffu));
+            v_next = __ldg(g.vel + ((uint32_t)e_next & 0x1fffffffu));
+        }
+        const int f = (int)(((uint32_t)e) >> 29);
+        const float3 tt = image3(xyz(pj), pi, k);
+        const float3 vj = (f & 4) ? xyz(vv) : make_float3(0.f, 0.f, 0.f);
+        acc_add<DIAG>(a, pi, tt, vj, f, (uint32_t)(e >> 32));
+    }
+}
+
 // One pass of a warp (all lanes call it together) over the candidates of its
 // lanes that still need one: the filter, the exact tests of the buffered
 // hits, and the accepted neighbours with ids above lo_id kept sorted in the
 // thread's column of sm.lst, at most kListA.  Those lanes then accumulate
 // their list; a lane that accepted more than the list held keeps need and
-// moves lo_id up to the last id it accumulated.
+// moves lo_id up to the last id it accumulated.  With ovf (this lane's row),
+// every accepted neighbour that leaves the list or never enters it is
+// appended there, up to kOvfCap of them, and counted in ovf_n.
 template <bool DIAG>
 __device__ __forceinline__ void sparse_pass(SparseSmem &sm, int t, uint32_t s, float3 pi, const Sight &sight,
                                             float dot_lim, uint32_t nc, bool &need, int64_t &lo_id, Acc &a,
-                                            const GridIn &g, const StepConst &k)
+                                            const GridIn &g, const StepConst &k, uint64_t *ovf, uint32_t &ovf_n)
 {
     const float3 vi = sight.v;
     const uint32_t mine = need ? nc : 0;
@@ -821,9 +852,18 @@ __device__ __forceinline__ void sparse_pass(SparseSmem &sm, int t, uint32_t s, f
                 ++more;
                 const uint64_t e = ((uint64_t)idj << 32) | (uint64_t)(jb | ((uint32_t)f << 29));
                 int w;
-                if (m < kListA) w = m++;
-                else if (e < sm.lst[kListA - 1][t]) w = kListA - 1;
-                else continue;
+                if (m < kListA) {
+                    w = m++;
+                } else {
+                    // the list is full: e or its last entry leaves it
+                    const uint64_t last = sm.lst[kListA - 1][t];
+                    w = e < last ? kListA - 1 : -1;
+                    if (ovf) {
+                        if (ovf_n < (uint32_t)kOvfCap) ovf[ovf_n] = w < 0 ? e : last;
+                        ++ovf_n;
+                    }
+                    if (w < 0) continue;
+                }
                 while (w > 0 && sm.lst[w - 1][t] > e) { sm.lst[w][t] = sm.lst[w - 1][t]; --w; }
                 sm.lst[w][t] = e;
             }
@@ -831,28 +871,37 @@ __device__ __forceinline__ void sparse_pass(SparseSmem &sm, int t, uint32_t s, f
         }
     }
     if (need) {
-        // the list's neighbours in id order, each loaded one entry ahead
-        uint64_t e_next = m > 0 ? sm.lst[0][t] : 0;
-        float4 p_next = make_float4(0.f, 0.f, 0.f, 0.f), v_next = p_next;
-        if (m > 0) {
-            p_next = __ldg(g.pos + ((uint32_t)e_next & 0x1fffffffu));
-            v_next = __ldg(g.vel + ((uint32_t)e_next & 0x1fffffffu));
-        }
-        for (int q = 0; q < m; ++q) {
-            const uint64_t e = e_next;
-            const float4 pj = p_next, vv = v_next;
-            if (q + 1 < m) {
-                e_next = sm.lst[q + 1][t];
-                p_next = __ldg(g.pos + ((uint32_t)e_next & 0x1fffffffu));
-                v_next = __ldg(g.vel + ((uint32_t)e_next & 0x1fffffffu));
-            }
-            const int f = (int)(((uint32_t)e) >> 29);
-            const float3 tt = image3(xyz(pj), pi, k);
-            const float3 vj = (f & 4) ? xyz(vv) : make_float3(0.f, 0.f, 0.f);
-            acc_add<DIAG>(a, pi, tt, vj, f, (uint32_t)(e >> 32));
-        }
+        list_accumulate<DIAG>(sm, t, m, pi, a, g, k);
         if (more <= (uint32_t)m) need = false;
         else lo_id = (int64_t)(sm.lst[m - 1][t] >> 32);
+    }
+}
+
+// A deferred boid's further passes from its overflow row (on <= kOvfCap
+// entries, every accepted neighbour with an id above lo_id): the next
+// kListA ids sorted in the thread's column of sm.lst and accumulated, until
+// none is left.  Per lane; no candidate is walked again.
+template <bool DIAG>
+__device__ __forceinline__ void ovf_passes(SparseSmem &sm, int t, const uint64_t *__restrict__ row, uint32_t on,
+                                           int64_t lo_id, float3 pi, Acc &a, const GridIn &g, const StepConst &k)
+{
+    for (;;) {
+        int m = 0;
+        uint32_t more = 0;
+        for (uint32_t q = 0; q < on; ++q) {
+            const uint64_t e = row[q];
+            if ((int64_t)(e >> 32) <= lo_id) continue;
+            ++more;
+            int w;
+            if (m < kListA) w = m++;
+            else if (e < sm.lst[kListA - 1][t]) w = kListA - 1;
+            else continue;
+            while (w > 0 && sm.lst[w - 1][t] > e) { sm.lst[w][t] = sm.lst[w - 1][t]; --w; }
+            sm.lst[w][t] = e;
+        }
+        list_accumulate<DIAG>(sm, t, m, pi, a, g, k);
+        if (more <= (uint32_t)m) return;
+        lo_id = (int64_t)(sm.lst[m - 1][t] >> 32);
     }
 }
 
@@ -910,7 +959,9 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
     acc_zero(a);
     int64_t lo_id = -1;  // ids <= lo_id were accumulated by earlier passes
     bool need = act;
-    sparse_pass<DIAG>(sm, t, s, pi, sight, dot_lim, nc, need, lo_id, a, g, k);
+    uint32_t ovf_n = 0;
+    sparse_pass<DIAG>(sm, t, s, pi, sight, dot_lim, nc, need, lo_id, a, g, k,
+                      o.ovf && act ? o.ovf + (size_t)s * kOvfCap : nullptr, ovf_n);
     if (o.defer) {
         // Boids with more accepted neighbours than one list holds go to
         // k_grid_sparse_more with their partial sums: every further pass
@@ -925,13 +976,14 @@ k_grid_sparse(GridIn g, GridOut o, StepConst kp, FlockTable ft)
             o.defer[2 * q] = s;
             o.defer[2 * q + 1] = (uint32_t)lo_id;
             o.carry[s] = a;
+            if (o.ovf) o.ovf_n[s] = ovf_n;
         } else if (act) {
             finish_boid<DIAG>(a, p4, sight.v, s, o, k);
         }
         return;
     }
     while (__any_sync(0xffffffffu, need))
-        sparse_pass<DIAG>(sm, t, s, pi, sight, dot_lim, nc, need, lo_id, a, g, k);
+        sparse_pass<DIAG>(sm, t, s, pi, sight, dot_lim, nc, need, lo_id, a, g, k, nullptr, ovf_n);
     if (act) finish_boid<DIAG>(a, p4, sight.v, s, o, k);
 }
 
@@ -976,12 +1028,19 @@ k_grid_sparse_more(GridIn g, GridOut o, StepConst kp, FlockTable ft)
         const float4 p4 = act ? g.pos[s] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 v4 = act ? g.vel[s] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float3 pi = xyz(p4);
-        const uint32_t nc = act ? sparse_segments(sm, t, pi, cell1(pi.y, k), cell1(pi.z, k), g, k) : 0;
+        // a boid whose first pass recorded all the neighbours it could not
+        // keep takes them from its overflow row; the others walk their
+        // candidates again
+        const uint32_t on = act && o.ovf ? o.ovf_n[s] : (uint32_t)kOvfCap + 1;
+        const bool from_row = on <= (uint32_t)kOvfCap;
+        if (from_row) ovf_passes<DIAG>(sm, t, o.ovf + (size_t)s * kOvfCap, on, lo_id, pi, a, g, k);
+        bool need = act && !from_row;
+        const uint32_t nc = need ? sparse_segments(sm, t, pi, cell1(pi.y, k), cell1(pi.z, k), g, k) : 0;
         const Sight sight = make_sight(xyz(v4));
         const float dot_lim = k.cone_pre ? -(sight.nv * k.dot_eps) : -INFINITY;
-        bool need = act;
+        uint32_t ovf_n = 0;
         while (__any_sync(0xffffffffu, need))
-            sparse_pass<DIAG>(sm, t, s, pi, sight, dot_lim, nc, need, lo_id, a, g, k);
+            sparse_pass<DIAG>(sm, t, s, pi, sight, dot_lim, nc, need, lo_id, a, g, k, nullptr, ovf_n);
         if (act) finish_boid<DIAG>(a, p4, sight.v, s, o, k);
     }
 }
@@ -2066,6 +2125,10 @@ cudaError_t launch_grid_force(const StepConst &k, const DevBuffers &b, int from,
     if (b.defer && b.defer_cnt && b.carry) {
         o.defer = b.defer;
         o.defer_cnt = b.defer_cnt;
+        if (b.ovf && b.ovf_n) {
+            o.ovf = b.ovf;
+            o.ovf_n = b.ovf_n;
+        }
     }
     if (diag) {
         o.dcnt = b.dcnt;
