@@ -521,8 +521,22 @@ int boids_create(const boids_params *params, boids_sim **out)
         }
         ALLOC(&b.dense_n, 3, true);
         ALLOC(&b.defer, 2 * n);
-        ALLOC(&b.ovf, (size_t)boidsgpu::kOvfCap * n);
-        ALLOC(&b.ovf_n, n);
+        // the deferred boids' overflow rows (196 B per boid) speed the
+        // further passes up and are optional: without them those passes
+        // walk the candidates again
+        if (n <= (size_t)1 << 26) {
+            uint64_t *rows = nullptr;
+            uint32_t *counts = nullptr;
+            if (cudaMalloc((void **)&rows, sizeof(uint64_t) * boidsgpu::kOvfCap * n) == cudaSuccess) {
+                if (cudaMalloc((void **)&counts, sizeof(uint32_t) * n) == cudaSuccess) {
+                    b.ovf = rows;
+                    b.ovf_n = counts;
+                } else {
+                    cudaFree(rows);
+                }
+            }
+            cudaGetLastError();
+        }
         b.defer_cnt = b.dense_n + 2;
         if (cudaStreamCreateWithFlags(&b.aux, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming) != cudaSuccess ||
