@@ -640,9 +640,9 @@ __global__ void k_grid_classify(const uint32_t *__restrict__ lstart,
 //
 // All lanes of a warp walk their own candidates in lock-step (a flat loop of
 // max-over-warp length).  Candidates passing the squared-distance filter are
-// buffered, and the whole warp runs the exact tests on its buffers together
-// whenever one of them is nearly full, so the expensive test runs with most
-// lanes busy.  The filter drops candidates behind the boid (the view-cone
+// buffered, and whenever one buffer is nearly full the warp runs the exact
+// tests of all its lanes' hits, dealt to its lanes 32 at a time whichever
+// lane found them, so the expensive test runs with nearly every lane busy.  The filter drops candidates behind the boid (the view-cone
 // pre-test, StepConst::dot_eps).  Accepted neighbours are kept sorted by id,
 // at most kListA per pass; a boid with more takes further passes, each
 // keeping the next kListA ids, so accumulation is always in ascending id --
@@ -830,27 +830,62 @@ __device__ __forceinline__ void sparse_pass(SparseSmem &sm, int t, uint32_t s, f
             if (vc[u]) filter(pc[u], qc[u], cc[u], sc[u]);
         // exact tests of the buffered hits, the whole warp together
         if (__any_sync(0xffffffffu, nb > kBufA - kCandStep) || it + kCandStep >= max_nc) {
-            // each entry's candidate is loaded one entry ahead, so that its
-            // load is in flight while the previous entry is tested
-            uint32_t wb_next = nb > 0 ? sm.buf[0][t] : 0u;
-            float4 pj_next = nb > 0 ? __ldg(g.pos + (wb_next & 0x7fffffffu)) : make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int q = 0; q < nb; ++q) {
-                const uint32_t wb = wb_next;
-                const uint32_t jb = wb & 0x7fffffffu;
-                const float4 pj = pj_next;
-                if (q + 1 < nb) {
-                    wb_next = sm.buf[q + 1][t];
-                    pj_next = __ldg(g.pos + (wb_next & 0x7fffffffu));
+            // The warp's hits are tested 32 at a time whatever lane found
+            // them (hit i of the lanes' buffers laid end to end goes to lane
+            // i % 32), so that a lane with many hits does not hold the warp
+            // for as many rounds; each verdict goes back into the finder's
+            // buffer (slot | rules << 29, rules 0: not accepted), and each
+            // lane then files its own accepted hits in its sorted list.
+            const int lane = t & 31, wbase = t & ~31;
+            int incl = nb;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            const int excl = incl - nb;
+            const int lo32 = (int)lo_id;  // ids are below 2^29
+            __syncwarp();  // the buffers are written
+            for (int base = 0; base < total; base += 32) {
+                const int i = base + lane;
+                int L = 0;  // the last lane whose hits start at or before i
+#pragma unroll
+                for (int st = 16; st > 0; st >>= 1) {
+                    const int e = __shfl_sync(0xffffffffu, excl, L + st);
+                    if (e <= i) L += st;
                 }
-                const uint32_t idj = __float_as_uint(pj.w);
-                if ((int64_t)idj <= lo_id) continue;
-                // a filter hit from a segment without periodic shift is nearer
-                // than F/2 on every axis: it is its own minimum image
-                const float3 tt = (wb >> 31) ? image3(xyz(pj), pi, k) : xyz(pj);
-                const int f = pair_flags(pi, sight, tt, k);
-                if (!f) continue;
+                const int q = i - __shfl_sync(0xffffffffu, excl, L);
+                const float3 po = make_float3(__shfl_sync(0xffffffffu, pi.x, L), __shfl_sync(0xffffffffu, pi.y, L),
+                                              __shfl_sync(0xffffffffu, pi.z, L));
+                Sight so;
+                so.v = make_float3(__shfl_sync(0xffffffffu, sight.v.x, L), __shfl_sync(0xffffffffu, sight.v.y, L),
+                                   __shfl_sync(0xffffffffu, sight.v.z, L));
+                so.nv = __shfl_sync(0xffffffffu, sight.nv, L);
+                so.inv_nv = __shfl_sync(0xffffffffu, sight.inv_nv, L);
+                const int olo = __shfl_sync(0xffffffffu, lo32, L);
+                if (i < total) {
+                    const uint32_t wb = sm.buf[q][wbase + L];
+                    const uint32_t jb = wb & 0x7fffffffu;
+                    const float4 pj = __ldg(g.pos + jb);
+                    int f = 0;
+                    if ((int)__float_as_uint(pj.w) > olo) {
+                        // a filter hit from a segment without periodic shift is
+                        // nearer than F/2 on every axis: its own minimum image
+                        const float3 tt = (wb >> 31) ? image3(xyz(pj), po, k) : xyz(pj);
+                        f = pair_flags(po, so, tt, k);
+                    }
+                    sm.buf[q][wbase + L] = jb | ((uint32_t)f << 29);
+                }
+            }
+            __syncwarp();  // the verdicts are written
+            for (int q = 0; q < nb; ++q) {
+                const uint32_t en = sm.buf[q][t];
+                if (!(en >> 29)) continue;
+                const uint32_t jb = en & 0x1fffffffu;
+                const uint32_t idj = __float_as_uint(__ldg(&g.pos[jb].w));
                 ++more;
-                const uint64_t e = ((uint64_t)idj << 32) | (uint64_t)(jb | ((uint32_t)f << 29));
+                const uint64_t e = ((uint64_t)idj << 32) | (uint64_t)en;
                 int w;
                 if (m < kListA) {
                     w = m++;
@@ -867,6 +902,7 @@ __device__ __forceinline__ void sparse_pass(SparseSmem &sm, int t, uint32_t s, f
                 while (w > 0 && sm.lst[w - 1][t] > e) { sm.lst[w][t] = sm.lst[w - 1][t]; --w; }
                 sm.lst[w][t] = e;
             }
+            __syncwarp();  // the buffers are free for the next hits
             nb = 0;
         }
     }
