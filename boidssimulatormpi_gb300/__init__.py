@@ -65,6 +65,7 @@ SIGNATURES = {
     "boids_init": (C.c_int, [_vp, C.c_char_p, C.c_int32]),
     "boids_init_ex": (C.c_int, [_vp, C.c_char_p, C.c_int32, C.c_int32]),
     "boids_set_state": (C.c_int, [_vp, _vp, _vp]),
+    "boids_set_population": (C.c_int, [_vp, C.c_uint32, _vp, _vp]),
     "boids_step": (C.c_int, [_vp, C.c_int32]),
     "boids_get_state": (C.c_int, [_vp, _vp, _vp]),
     "boids_get_forces": (C.c_int, [_vp, _vp]),
@@ -162,7 +163,8 @@ class BoidSimulation:
         self.record_forces = record_forces
         self.allpairs_kernels = allpairs_kernels
         self.h = None
-        self.N = 0
+        self.N = 0          # number_of_agents: the handle's capacity
+        self.n_active = 0   # the population the getters cover (N, or set_population's n)
         self._cache = None
 
     # -- BoidSimulation::setup (src/boid_simulation.h:19-33)
@@ -183,7 +185,7 @@ class BoidSimulation:
         _check(lib().boids_create(C.byref(p), C.byref(h)))
         self.h = h
         self.params = p
-        self.N = number_of_agents
+        self.N = self.n_active = number_of_agents
         self.field_size_X = self.field_size_Y = self.field_size_Z = float(field_size)
         self.initialization_type = initialization
         self.rand_seed = rand_seed
@@ -193,6 +195,7 @@ class BoidSimulation:
     # -- BoidSimulation::init
     def init(self, seed_mode: int = -1):
         _check(lib().boids_init_ex(self.h, self.initialization_type.encode(), self.rand_seed, seed_mode))
+        self.n_active = self.N
         self._cache = None
 
     # -- BoidSimulation::update
@@ -205,38 +208,55 @@ class BoidSimulation:
     def set_state(self, pos, vel):
         pos, vel = _f32(pos, 3 * self.N), _f32(vel, 3 * self.N)
         _check(lib().boids_set_state(self.h, _ptr(pos), _ptr(vel)))
+        self.n_active = self.N
+        self._cache = None
+
+    def set_population(self, pos, vel):
+        """The state of the first n boids, n = len(pos) // 3 (at most N)."""
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1)
+        vel = np.ascontiguousarray(vel, dtype=np.float32).reshape(-1)
+        if pos.size % 3 or vel.size != pos.size:
+            raise ValueError("positions and velocities must both hold 3 floats per boid")
+        _check(lib().boids_set_population(self.h, pos.size // 3, _ptr(pos), _ptr(vel)))
+        self.n_active = pos.size // 3
         self._cache = None
 
     def state(self, pos_out=None, vel_out=None):
-        """(pos, vel) as float32 arrays of shape (N, 3), id order."""
-        pos = np.empty(3 * self.N, np.float32) if pos_out is None else pos_out
-        vel = np.empty(3 * self.N, np.float32) if vel_out is None else vel_out
+        """(pos, vel) as float32 arrays of shape (n, 3), id order: n = N, or
+        the population last set by set_population."""
+        n = self.n_active
+        pos = np.empty(3 * n, np.float32) if pos_out is None else pos_out
+        vel = np.empty(3 * n, np.float32) if vel_out is None else vel_out
         _check(lib().boids_get_state(self.h, _ptr(pos), _ptr(vel)))
-        return pos.reshape(self.N, 3), vel.reshape(self.N, 3)
+        return pos.reshape(n, 3), vel.reshape(n, 3)
 
     def positions(self, out=None):
-        pos = np.empty(3 * self.N, np.float32) if out is None else out
+        n = self.n_active
+        pos = np.empty(3 * n, np.float32) if out is None else out
         _check(lib().boids_get_state(self.h, _ptr(pos), None))
-        return pos.reshape(self.N, 3)
+        return pos.reshape(n, 3)
 
     def forces(self):
-        """get_force for all ids: (N, 9) = cohesion xyz, separation xyz, alignment xyz."""
-        f = np.empty(9 * self.N, np.float32)
+        """get_force for all ids: (n, 9) = cohesion xyz, separation xyz, alignment xyz."""
+        n = self.n_active
+        f = np.empty(9 * n, np.float32)
         _check(lib().boids_get_forces(self.h, _ptr(f)))
-        return f.reshape(self.N, 9)
+        return f.reshape(n, 9)
 
     def cells(self):
-        """Boid::grid_index[8] of every boid, (N, 8) int32."""
-        g = np.empty(8 * self.N, np.int32)
+        """Boid::grid_index[8] of every boid, (n, 8) int32."""
+        n = self.n_active
+        g = np.empty(8 * n, np.int32)
         _check(lib().boids_get_cells(self.h, _ptr(g)))
-        return g.reshape(self.N, 8)
+        return g.reshape(n, 8)
 
     def neighbor_sets(self):
-        """(count, hash), each (N, 3): per rule (cohesion, separation, alignment)."""
-        c = np.empty(3 * self.N, np.int32)
-        h = np.empty(3 * self.N, np.uint64)
+        """(count, hash), each (n, 3): per rule (cohesion, separation, alignment)."""
+        n = self.n_active
+        c = np.empty(3 * n, np.int32)
+        h = np.empty(3 * n, np.uint64)
         _check(lib().boids_get_neighbor_sets(self.h, _ptr(c), _ptr(h)))
-        return c.reshape(self.N, 3), h.reshape(self.N, 3)
+        return c.reshape(n, 3), h.reshape(n, 3)
 
     def grid_info(self) -> dict:
         gi = GridInfo()

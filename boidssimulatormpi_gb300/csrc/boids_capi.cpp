@@ -594,7 +594,7 @@ void boids_destroy(boids_sim *s)
 namespace {
 
 // First id of transfer piece c (of kXferChunks), on a 1024-id boundary.
-uint32_t xfer_start(uint32_t n, int c)
+static uint32_t xfer_start(uint32_t n, int c)
 {
     const uint64_t b = ((uint64_t)n * (uint32_t)c / boids_sim::kXferChunks + 1023) & ~(uint64_t)1023;
     return (uint32_t)std::min<uint64_t>(b, n);
@@ -602,7 +602,7 @@ uint32_t xfer_start(uint32_t n, int c)
 
 // Whether the transfers run in pieces: with the side stream, once the
 // pieces' events exist (made on first use; without them, one piece).
-bool xfer_pipelined(boids_sim *s)
+static bool xfer_pipelined(boids_sim *s)
 {
     if (!s->b.aux) return false;
     for (cudaEvent_t &ev : s->xfer_ev)
@@ -614,13 +614,16 @@ bool xfer_pipelined(boids_sim *s)
     return true;
 }
 
-bool graph_ready(boids_sim *s, bool rec, int which);
+static bool graph_ready(boids_sim *s, bool rec, int which);
 
 }  // namespace
 
-int boids_set_state(boids_sim *s, const float *pos3n, const float *vel3n)
+namespace {
+
+// boids_set_state for the current population s->k.n.
+static int set_state_n(boids_sim *s, const float *pos3n, const float *vel3n)
 {
-    if (!s || (!pos3n && s->k.n) || (!vel3n && s->k.n)) return fail(BOIDS_EINVAL, "boids_set_state: null argument");
+    if ((!pos3n && s->k.n) || (!vel3n && s->k.n)) return fail(BOIDS_EINVAL, "boids_set_state: null argument");
     int rc = use_device(s);
     if (rc) return rc;
     const uint32_t n = s->k.n;
@@ -680,10 +683,30 @@ int boids_set_state(boids_sim *s, const float *pos3n, const float *vel3n)
     return BOIDS_OK;
 }
 
+}  // namespace
+
+int boids_set_state(boids_sim *s, const float *pos3n, const float *vel3n)
+{
+    if (!s) return fail(BOIDS_EINVAL, "boids_set_state: null argument");
+    s->k.n = s->p.number_of_agents;  // the whole population
+    return set_state_n(s, pos3n, vel3n);
+}
+
+int boids_set_population(boids_sim *s, uint32_t n, const float *pos3n, const float *vel3n)
+{
+    if (!s) return fail(BOIDS_EINVAL, "boids_set_population: null handle");
+    if (n > s->p.number_of_agents)
+        return fail(BOIDS_EINVAL, "boids_set_population: more boids than the handle was created for");
+    s->has_state = false;
+    s->forces_valid = false;
+    s->k.n = n;
+    return set_state_n(s, pos3n, vel3n);
+}
+
 int boids_init_ex(boids_sim *s, const char *init, int32_t seed, int32_t seed_mode)
 {
     if (!s || !init) return fail(BOIDS_EINVAL, "boids_init: null argument");
-    const uint32_t n = s->k.n;
+    const uint32_t n = s->p.number_of_agents;  // the whole population, whatever boids_set_population left
     std::vector<float> pos((size_t)3 * n), vel((size_t)3 * n);
     const std::string kind(init);
     if (kind == "test" || kind == "random_uniform") {
@@ -716,7 +739,7 @@ namespace {
 constexpr int kGraphSteps = 16;  // updates per captured graph
 
 // One update: BoidSimulation::update of the grid or all-pairs engine.
-int step_once(boids_sim *s, bool rec)
+static int step_once(boids_sim *s, bool rec)
 {
     if (s->engine == 1) {
         {
@@ -742,7 +765,7 @@ int step_once(boids_sim *s, bool rec)
 // Graph `which` (0: kGraphSteps updates, 1: one update) for the handle's
 // current stream, buffer parity and constants, captured if needed; false
 // when it cannot be had.
-bool graph_ready(boids_sim *s, bool rec, int which)
+static bool graph_ready(boids_sim *s, bool rec, int which)
 {
     if (s->graph_off || !s->stream) return false;  // the legacy stream cannot be captured
     boids_sim::StepGraph &gr = s->graphs[which];
@@ -977,7 +1000,7 @@ int boids_frame_async(boids_sim *s, float *pframe, float *vframe, int32_t with_f
     int rc = use_device(s);
     if (rc) return rc;
     const size_t n = s->k.n;
-    if (!s->frame_dev && (rc = dalloc(&s->frame_dev, 15 * n))) return rc;
+    if (!s->frame_dev && (rc = dalloc(&s->frame_dev, (size_t)15 * s->p.number_of_agents))) return rc;
     if (!s->frame_ev[slot]) CK(cudaEventCreateWithFlags(&s->frame_ev[slot], cudaEventDisableTiming));
     const size_t stride = with_forces ? 12 : 3;
     float *dp = s->frame_dev, *dv = s->frame_dev + 12 * n;
@@ -1026,7 +1049,7 @@ int boids_get_cells(boids_sim *s, int32_t *gi8)
     if (!s->has_state) return fail(BOIDS_ESTATE, "boids_get_cells: no state");
     int rc = use_device(s);
     if (rc) return rc;
-    if (!s->b.cells8 && (rc = dalloc(&s->b.cells8, (size_t)8 * s->k.n))) return rc;
+    if (!s->b.cells8 && (rc = dalloc(&s->b.cells8, (size_t)8 * s->p.number_of_agents))) return rc;
     CK(boidsgpu::launch_ref_cells(s->k, s->b.pos[s->cur], s->b.cells8, s->stream, &s->launches));
     CK(cudaMemcpyAsync(gi8, s->b.cells8, sizeof(int32_t) * 8 * s->k.n, cudaMemcpyDeviceToHost, s->stream));
     return boids_synchronize(s);
@@ -1038,9 +1061,9 @@ int boids_get_neighbor_sets(boids_sim *s, int32_t *count3n, uint64_t *hash3n)
     if (!s->has_state) return fail(BOIDS_ESTATE, "boids_get_neighbor_sets: no state");
     int rc = use_device(s);
     if (rc) return rc;
-    const size_t n = s->k.n;
-    if (!s->b.dcnt && (rc = dalloc(&s->b.dcnt, 3 * n))) return rc;
-    if (!s->b.dhash && (rc = dalloc(&s->b.dhash, 3 * n))) return rc;
+    const size_t n = s->k.n, cap = s->p.number_of_agents;  // sized once for the largest population
+    if (!s->b.dcnt && (rc = dalloc(&s->b.dcnt, 3 * cap))) return rc;
+    if (!s->b.dhash && (rc = dalloc(&s->b.dhash, 3 * cap))) return rc;
     if (s->engine == 1) {
         CK(boidsgpu::launch_grid_scan(s->k, s->b, s->stream, &s->launches));
         CK(boidsgpu::launch_grid_scatter(s->k, s->b, s->cur, false, s->stream, &s->launches));

@@ -127,8 +127,17 @@ int boids_init(boids_sim *sim, const char *initialization, int32_t rand_seed);
 int boids_init_ex(boids_sim *sim, const char *initialization, int32_t rand_seed, int32_t seed_mode);
 
 /* Boid::set_serialized_data for every boid (src/boid.cpp:68-76): uploads a
- * state in id order.  The grid engine requires 0 <= x,y,z <= field_size. */
+ * state of number_of_agents boids in id order.  The grid engine requires
+ * 0 <= x,y,z <= field_size. */
 int boids_set_state(boids_sim *sim, const float *pos3n, const float *vel3n);
+
+/* The state of a population of n boids, n at most the number_of_agents the
+ * handle was created with: boids_set_state for the first n ids.  For a
+ * domain-decomposed flock, whose rank-local boids (its block's and the
+ * margin's, cf. BoidSimulationMultiNode, src/boid_simulation_mpi.cpp:151-243)
+ * change in number every update.  The getters, frames and updates then
+ * cover those n; boids_init sets the whole population again. */
+int boids_set_population(boids_sim *sim, uint32_t n, const float *pos3n, const float *vel3n);
 
 /* BoidSimulation::update (src/boid_simulation_grid.cpp:165-293), `steps`
  * times.  Asynchronous on the handle's stream.  A call of 32 or more steps
