@@ -1,9 +1,11 @@
 """The domain-decomposed flock (boidssimulatormpi_gb300/halo.py, the
 counterpart of BoidSimulationMultiNode, src/boid_simulation_mpi.cpp) on CPU:
-gloo process groups of 2, 3 and 4 ranks, each rank's local update done by
-the oracle's port of src/boid_simulation_grid.cpp; after 30 updates the
-gathered flock equals one port holding the whole flock, bit for bit.  Also
-the block and margin arithmetic against a direct check."""
+gloo process groups of 2, 3, 4 and 8 ranks, each rank's local update done by
+the oracle's port of src/boid_simulation_grid.cpp; the gathered flock equals
+one port holding the whole flock, bit for bit (30 updates of 3000 boids;
+and the reference's test/compare_mpi.sh, which compares 8 MPI ranks with the
+serial engine: N=1000, T=100, settings/test.ini).  Also the block and
+margin arithmetic against a direct check."""
 import os
 import socket
 import sys
@@ -17,6 +19,7 @@ torch = pytest.importorskip("torch")
 
 MARUN2019 = dict(sep=(0.01, 0.5, 0.002), ali=(0.05, 0.3333333333333333, 0.06),
                  coh=(0.05, 0.5, 0.008), vmax=0.005, vmin=0.001)
+TEST_INI = dict(sep=(0.1, 0.9, 0.0001), ali=(0.1, 0.7, 0.1), coh=(0.1, 0.8, 0.1), vmax=0.003, vmin=0.001)
 
 
 def _collect(q, procs, limit=300):
@@ -68,11 +71,13 @@ class PortEngine:
         return np.asarray(self.f, np.float32).reshape(-1, 9)
 
 
-def _start(n, field, seed, gathered):
+def _start(n, field, seed, gathered, m=MARUN2019):
     sys.path.insert(0, ROOT)
     import oracle as O
-    m = MARUN2019
     p = O.params(n, field, m["sep"], m["ali"], m["coh"], m["vmax"], m["vmin"])
+    if gathered == "test":  # the reference's `test` placement, never seeded (boidsim)
+        pos, vel = O.init_state(p, "test", False, seed)
+        return O, p, pos, vel
     pos, vel = O.init_state(p, "random_uniform", True, seed)
     if gathered:  # boids bunched around points on block edges and corners
         rng = np.random.default_rng(seed)
@@ -88,9 +93,9 @@ def _worker(rank, world, port, topology, n, field, steps, gathered, q):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        O, p, pos, vel = _start(n, field, 7, gathered)
+        m = TEST_INI if gathered == "test" else MARUN2019
+        O, p, pos, vel = _start(n, field, 7, gathered, m)
         from boidssimulatormpi_gb300.halo import HaloFlock
-        m = MARUN2019
         hf = HaloFlock(n, field, m["sep"], m["ali"], m["coh"], m["vmax"], m["vmin"],
                        engine=PortEngine(O, field, m), group=dist.group.WORLD, topology=topology)
         hf.set_global_state(pos, vel)
@@ -103,11 +108,13 @@ def _worker(rank, world, port, topology, n, field, steps, gathered, q):
         dist.destroy_process_group()
 
 
-@pytest.mark.parametrize("world,topology,gathered", [(2, (1, 1, 2), False), (3, (1, 1, 3), True),
-                                                     (4, (1, 2, 2), True)])
-def test_decomposed_flock_equals_one_engine(world, topology, gathered):
+@pytest.mark.parametrize("world,topology,gathered,n,steps", [
+    (2, (1, 1, 2), False, 3000, 30), (3, (1, 1, 3), True, 3000, 30), (4, (1, 2, 2), True, 3000, 30),
+    # test/compare_mpi.sh: 8 ranks, N=1000, T=100, settings/test.ini (test placement)
+    (8, (2, 2, 2), "test", 1000, 100)])
+def test_decomposed_flock_equals_one_engine(world, topology, gathered, n, steps):
     import torch.multiprocessing as mp
-    n, field, steps = 3000, 1.0, 30
+    field = 1.0
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
@@ -122,7 +129,7 @@ def test_decomposed_flock_equals_one_engine(world, topology, gathered):
     gp = np.frombuffer(got[0], np.float32).reshape(-1)
     gv = np.frombuffer(got[1], np.float32).reshape(-1)
     assert 0 < got[2] < n  # rank 0 holds a part of the flock
-    O, p, pos, vel = _start(n, field, 7, gathered)
+    O, p, pos, vel = _start(n, field, 7, gathered, TEST_INI if gathered == "test" else MARUN2019)
     op, ov = pos.copy(), vel.copy()
     O.GridPort(p, op).step(op, ov, steps, forces=False)
     assert np.array_equal(gp.view(np.uint32), op.view(np.uint32)), "positions"
