@@ -242,31 +242,46 @@ class HaloFlock:
         own = self._owned()
         return self.ids[own], self.pos[own], self.vel[own]
 
-    def gather(self):
-        """The whole flock in id order, (pos, vel) of shape (N, 3), on every
-        rank (all_gather of the owned boids, padded to the largest count)."""
-        ids, p, v = self.owned_state()
-        if not (self.multi and self.size > 1):
-            order = np.argsort(ids)
-            return p[order], v[order]
-        import torch
-        dist = self.dist
-        dev = torch.device("cuda", torch.cuda.current_device()) \
-            if dist.get_backend(self.group) == "nccl" else torch.device("cpu")
-        rows = np.concatenate([ids.astype(np.int64).view(np.float32).reshape(-1, 2), p, v], 1) \
-            if len(ids) else np.zeros((0, 8), np.float32)
-        cnt = torch.tensor([len(ids)], dtype=torch.int64, device=dev)
-        cnts = [torch.empty_like(cnt) for _ in range(self.size)]
-        dist.all_gather(cnts, cnt, group=self.group)
-        cmax = int(max(int(c.item()) for c in cnts))
-        buf = torch.zeros(cmax * 8, dtype=torch.float32, device=dev)
-        buf[:rows.size] = torch.from_numpy(np.ascontiguousarray(rows).reshape(-1)).to(dev)
-        outs = [torch.empty_like(buf) for _ in range(self.size)]
-        dist.all_gather(outs, buf, group=self.group)
-        parts = [o.cpu().numpy().reshape(-1, 8)[:int(c.item())] for o, c in zip(outs, cnts)]
-        allr = np.concatenate(parts)
-        gid = np.ascontiguousarray(allr[:, :2]).view(np.int64).reshape(-1)
+    def _gather_rows(self, ids: np.ndarray, vals: np.ndarray) -> np.ndarray:
+        """Rows vals (one per id, float32) of every rank's ids, in id order
+        over the whole flock, on every rank (all_gather, padded to the
+        largest count)."""
+        vals = np.asarray(vals, np.float32).reshape(len(ids), -1)
+        width = 2 + vals.shape[1]
+        rows = np.concatenate([ids.astype(np.int64).view(np.float32).reshape(-1, 2), vals], 1) \
+            if len(ids) else np.zeros((0, width), np.float32)
+        if self.multi and self.size > 1:
+            import torch
+            dist = self.dist
+            dev = torch.device("cuda", torch.cuda.current_device()) \
+                if dist.get_backend(self.group) == "nccl" else torch.device("cpu")
+            cnt = torch.tensor([len(ids)], dtype=torch.int64, device=dev)
+            cnts = [torch.empty_like(cnt) for _ in range(self.size)]
+            dist.all_gather(cnts, cnt, group=self.group)
+            cmax = int(max(int(c.item()) for c in cnts))
+            buf = torch.zeros(cmax * width, dtype=torch.float32, device=dev)
+            buf[:rows.size] = torch.from_numpy(np.ascontiguousarray(rows).reshape(-1)).to(dev)
+            outs = [torch.empty_like(buf) for _ in range(self.size)]
+            dist.all_gather(outs, buf, group=self.group)
+            rows = np.concatenate([o.cpu().numpy().reshape(-1, width)[:int(c.item())] for o, c in zip(outs, cnts)])
+        gid = np.ascontiguousarray(rows[:, :2]).view(np.int64).reshape(-1)
         if gid.size != self.N or np.any(np.sort(gid) != np.arange(self.N)):
             raise RuntimeError("the ranks do not own every boid exactly once")
-        order = np.argsort(gid)
-        return allr[order, 2:5].copy(), allr[order, 5:8].copy()
+        return rows[np.argsort(gid), 2:].copy()
+
+    def gather(self):
+        """The whole flock in id order, (pos, vel) of shape (N, 3), on every
+        rank (the reference's gather_data: MPI_Gather and a sort by id,
+        src/boid_simulation_mpi.cpp:555-586)."""
+        ids, p, v = self.owned_state()
+        r = self._gather_rows(ids, np.concatenate([p, v], 1))
+        return r[:, 0:3], r[:, 3:6]
+
+    def gather_forces(self):
+        """get_force of the last update for every boid, (N, 9) in id order
+        (cohesion, separation, alignment xyz), on every rank; needs an
+        engine that records forces."""
+        if self.force is None:
+            raise RuntimeError("no forces: no update yet, or an engine without force recording")
+        ids, f = self.force
+        return self._gather_rows(ids, f)

@@ -102,8 +102,9 @@ def _worker(rank, world, port, topology, n, field, steps, gathered, q):
         local0 = len(hf.ids)
         hf.update(steps)
         gp, gv = hf.gather()
+        gf = hf.gather_forces()
         if rank == 0:
-            q.put((gp.tobytes(), gv.tobytes(), local0))
+            q.put((gp.tobytes(), gv.tobytes(), local0, gf.tobytes()))
     finally:
         dist.destroy_process_group()
 
@@ -131,9 +132,11 @@ def test_decomposed_flock_equals_one_engine(world, topology, gathered, n, steps)
     assert 0 < got[2] < n  # rank 0 holds a part of the flock
     O, p, pos, vel = _start(n, field, 7, gathered, TEST_INI if gathered == "test" else MARUN2019)
     op, ov = pos.copy(), vel.copy()
-    O.GridPort(p, op).step(op, ov, steps, forces=False)
+    of = np.asarray(O.GridPort(p, op).step(op, ov, steps, forces=True), np.float32).reshape(-1)
+    gf = np.frombuffer(got[3], np.float32)
     assert np.array_equal(gp.view(np.uint32), op.view(np.uint32)), "positions"
     assert np.array_equal(gv.view(np.uint32), ov.view(np.uint32)), "velocities"
+    assert np.array_equal(gf.view(np.uint32), of.view(np.uint32)), "forces of the last update"
 
 
 def test_dims_create_balances():
