@@ -186,3 +186,33 @@ def test_destinations_are_the_regions_that_hold_a_boid(topology):
     own = dec.owners(pos)
     assert all((i, int(own[i])) in got for i in range(len(pos)))
     assert got == want
+
+
+def test_blocks_thinner_than_twice_the_margin_are_refused():
+    sys.path.insert(0, ROOT)
+    from boidssimulatormpi_gb300.halo import Decomposition
+    Decomposition(1.0, (1, 1, 5), 0.1)          # 0.2 thick: enough
+    with pytest.raises(ValueError, match="thinner"):
+        Decomposition(1.0, (1, 1, 6), 0.1)      # 0.167 thick
+    with pytest.raises(ValueError, match="positive"):
+        Decomposition(1.0, (1, 0, 2), 0.1)
+
+
+def test_single_rank_keeps_every_boid():
+    """Without a process group the flock is one block: every boid is owned
+    and nothing is exchanged; the updates equal the port's."""
+    sys.path.insert(0, ROOT)
+    from boidssimulatormpi_gb300.halo import HaloFlock
+    n, field = 500, 0.8
+    O, p, pos, vel = _start(n, field, 11, False)
+    m = MARUN2019
+    hf = HaloFlock(n, field, m["sep"], m["ali"], m["coh"], m["vmax"], m["vmin"],
+                   engine=PortEngine(O, field, m))
+    hf.set_global_state(pos, vel)
+    assert len(hf.ids) == n
+    hf.update(5)
+    gp, gv = hf.gather()
+    op, ov = pos.copy(), vel.copy()
+    O.GridPort(p, op).step(op, ov, 5, forces=False)
+    assert np.array_equal(gp.reshape(-1).view(np.uint32), op.view(np.uint32))
+    assert np.array_equal(gv.reshape(-1).view(np.uint32), ov.view(np.uint32))
