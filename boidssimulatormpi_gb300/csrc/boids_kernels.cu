@@ -15,12 +15,14 @@
 // classification of every full-size cell -> rule kernels that split the
 // boids by the occupancy of their cell:
 //   k_grid_sparse  one thread per boid; candidates of the 27 cells around it
-//                  are filtered, exactly tested, and kept sorted by id; boids
-//                  that need more than one pass are queued for
+//                  are filtered, exactly tested (the warp's hits dealt to all
+//                  its lanes), and kept sorted by id; boids that need more
+//                  than one pass are queued, with the neighbours their list
+//                  could not keep, for
 //   k_grid_sparse_more, which runs their further passes in full warps beside
 //   k_grid_dense   one CTA per crowded cell; the 27-cell candidates are
-//                  radix-sorted by id once in shared memory and every boid of
-//                  the cell walks them in that order.
+//                  sorted by id once in shared memory, the exact tests mark
+//                  rule masks, and ordered sums walk the masks in id order.
 // Both integrate, write the new state in place of the sorted slot and bin it
 // for the next step (cell key + rank from an atomic count).
 #include "boids_engine.h"
