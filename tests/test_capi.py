@@ -81,6 +81,9 @@ def test_null_arguments(boids_lib):
     assert L.boids_create(None, None) == -1
     assert L.boids_step(None, 1) == -1
     assert L.boids_get_state(None, None, None) == -1
+    assert L.boids_set_state(None, None, None) == -1
+    assert L.boids_set_population(None, 0, None, None) == -1
+    assert b"null handle" in L.boids_last_error()
     assert L.boids_step_noalloc(None, None, None, None, None, None) == -1
 
 
