@@ -87,38 +87,46 @@ class Decomposition:
     def owners(self, pos: np.ndarray) -> np.ndarray:
         return self.rank_of(self.blocks(pos))
 
+    # the 26 offsets from a block to its neighbours
+    _OFF = np.array([[ox, oy, oz] for ox in (-1, 0, 1) for oy in (-1, 0, 1) for oz in (-1, 0, 1)
+                     if (ox, oy, oz) != (0, 0, 0)])
+
     def destinations(self, pos: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         """(boid index, rank) pairs: every rank whose block or margin holds
-        the boid, its owner included, each pair once."""
-        pos = np.asarray(pos, np.float64)
+        the boid, its owner first, each pair once."""
+        pos = np.asarray(pos, np.float64).reshape(-1, 3)
+        n = pos.shape[0]
         d = np.asarray(self.dims)
         w = self.F / d
         b = self.blocks(pos)
+        owner = self.rank_of(b)
+        # only boids within the margin of a face between two blocks reach
+        # another block: the others go to their owner alone
         lo = b * w
-        near_lo = (pos - lo) < self.margin          # also in the margin of block b - 1
-        near_hi = (lo + w - pos) <= self.margin     # ... of block b + 1
-        idx, ranks = [], []
-        n = pos.shape[0]
-        for ox in (-1, 0, 1):
-            for oy in (-1, 0, 1):
-                for oz in (-1, 0, 1):
-                    off = np.array([ox, oy, oz])
-                    if np.any((off != 0) & (d == 1)):
-                        continue
-                    m = np.ones(n, bool)
-                    for a in range(3):
-                        if off[a] < 0:
-                            m &= near_lo[:, a]
-                        elif off[a] > 0:
-                            m &= near_hi[:, a]
-                    sel = np.nonzero(m)[0]
-                    if sel.size:
-                        idx.append(sel)
-                        ranks.append(self.rank_of((b[sel] + off) % d))
-        if not idx:
-            return np.zeros(0, np.int64), np.zeros(0, np.int64)
-        pairs = np.unique(np.stack([np.concatenate(idx), np.concatenate(ranks)], 1), axis=0)
-        return pairs[:, 0], pairs[:, 1]
+        near_lo = ((pos - lo) < self.margin) & (d > 1)         # also in the margin of block b - 1
+        near_hi = ((lo + w - pos) <= self.margin) & (d > 1)    # ... of block b + 1
+        edge = np.nonzero(np.any(near_lo | near_hi, axis=1))[0]
+        ei, er = [], []
+        for off in self._OFF:
+            if np.any((off != 0) & (d == 1)):
+                continue
+            m = np.ones(edge.size, bool)
+            for a in range(3):
+                if off[a] < 0:
+                    m &= near_lo[edge, a]
+                elif off[a] > 0:
+                    m &= near_hi[edge, a]
+            sel = edge[m]
+            if sel.size:
+                ei.append(sel)
+                er.append(self.rank_of((b[sel] + off) % d))
+        if ei:
+            # a blocks-of-two axis reaches the same neighbour both ways: each pair once
+            key = np.unique(np.concatenate(ei).astype(np.int64) * self.size + np.concatenate(er))
+            ei, er = key // self.size, key % self.size
+        else:
+            ei, er = np.zeros(0, np.int64), np.zeros(0, np.int64)
+        return np.concatenate([np.arange(n, dtype=np.int64), ei]), np.concatenate([owner.astype(np.int64), er])
 
 
 class HaloFlock:
